@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""ε-self-join benchmark: prints one JSON line.
+
+Workload (default): the SUSY-shaped low-dimensional join, n = 5,000,000
+points, d = 18, FP64, k = 6 reference points, ε calibrated for a mean of 64
+neighbours (seeded synthetic stand-in: the real SUSY file is not available).
+
+One step = one complete self-join through the library's C ABI (index build,
+neighbour enumeration, join with pair compaction; the full pair list is
+written), i.e. the work the reference's nodeLauncher5 does per dataset.
+
+  value  points joined per second with the input resident in HBM and the
+         pair list written to a device buffer (CUDA events on the library's
+         stream, which is torch's current stream).
+  e2e    the same metric through the same call with a host input array and
+         the pair list returned in host memory (host->device copy of the
+         points and device->host copy of the pairs inside the timed region).
+
+Also reported: wall time per join, distance evaluations/s (unordered
+candidate pairs the join evaluated / step time), pairs/s, the plain FP64
+CUDA-core join on the same index (identical pair set required), the roofline
+of the dominant kernel and a CPU baseline (the reference's brute-force
+algorithm, src/utils.cu:285-317, as the oracle's C port, on a bounded row
+sample, extrapolated to the whole job).
+
+`--impl reference` times that CPU implementation alone (rank 0 only).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "self-join-mistic_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+from mistic import workloads as W  # noqa: E402
+
+METRIC = "self-join wall time & distance evals/s: mixed-prec vs FP64 plain, exact pair set"
+UNIT = "points/s"
+
+#: workload name -> (constructor, description)
+WORKLOADS = {
+    "susy18": (lambda n: W.susy18(n or 5_000_000),
+               "SUSY-shaped n=5e6 d=18 FP64, k=6, 64 mean neighbours"),
+    "uniform18": (lambda n: W.uniform18(n or 100_000),
+                  "uniform n=1e5 d=18 FP64, k=6, 32 mean neighbours"),
+}
+
+FALLBACK_PEAKS = {"hbm_gbs": 6785.9, "bf16_tflops": 1922.1, "bf16_tflops_sustained": 1711.2}
+
+
+def load_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        d["_source"] = "MEASURED_PEAKS.json"
+        return d
+    except Exception:
+        d = dict(FALLBACK_PEAKS)
+        d["_source"] = "MEASURED_PEAKS.json values recorded at build time"
+        return d
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                c = [x.strip() for x in line.split(",")]
+                if len(c) < 9:
+                    continue
+                try:
+                    sm.append(float(c[1]))
+                    smax.append(float(c[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, c[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU baseline
+def cpu_sample(x: np.ndarray, eps: float, seconds: float) -> dict:
+    """The reference's brute-force algorithm (oracle C port, all host
+    threads) on rows [0, R) against all n rows; R grows until the sample takes
+    about `seconds`.  Extrapolates to the whole n x n job."""
+    from oracle import oracle as O
+    threads = O.max_threads()
+    n = x.shape[0]
+    rows = max(threads, 16)
+    t = 0.0
+    while True:
+        t0 = time.perf_counter()
+        O.count_rows(x, eps, 0, min(rows, n), threads)
+        t = time.perf_counter() - t0
+        if t >= seconds / 4 or rows >= n:
+            break
+        rows = min(n, int(rows * max(2.0, seconds / 4 / max(t, 1e-3))))
+    rows = min(n, max(rows, int(rows * seconds / max(t, 1e-6))))
+    t0 = time.perf_counter()
+    O.count_rows(x, eps, 0, rows, threads)
+    t = time.perf_counter() - t0
+    job_s = t * n / rows
+    return {"rows": rows, "seconds": t, "job_seconds": job_s, "threads": threads,
+            "points_per_s": n / job_s, "evals_per_s": rows * n / t}
+
+
+# ------------------------------------------------------------------ arms
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def run_reference(args, wl) -> None:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    x, eps = wl.pts, wl.eps
+    per_step = args.ref_seconds
+    for _ in range(args.warmup):
+        cpu_sample(x, eps, per_step / 4)
+    samples = [cpu_sample(x, eps, per_step) for _ in range(args.steps)]
+    job = statistics.mean(s["job_seconds"] for s in samples)
+    value = wl.n / job
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": job * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "n": wl.n, "d": wl.d, "k": wl.k,
+                   "eps_hex": float(wl.eps).hex(), "desc": WORKLOADS[args.workload][1]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": samples[0]["threads"], "kind": "port",
+                         "sample": f"rows [0,{samples[0]['rows']}) x all {wl.n} rows per step, "
+                                   "extrapolated to n rows; brute_force of src/utils.cu:285-317 "
+                                   "(oracle C port, OpenMP)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_mistic(args, wl) -> None:
+    import torch
+    import mistic
+    from mistic import _lib as L
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    h = mistic.Handle(local, stream=stream.cuda_stream)
+
+    x = np.ascontiguousarray(wl.pts)
+    n, d = x.shape
+    dt = L.F64 if x.dtype == np.float64 else L.F32
+    xt = torch.from_numpy(x).to(dev)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # first call sizes the caller-owned device pair buffer
+    r0 = h.to_result(h.selfjoin_raw(xt.data_ptr(), n, d, dt, wl.k, wl.eps,
+                                    h.opts(input_on_device=True)))
+    cap = int(r0.pairs_ij * 1.02) + 1024
+    pbuf = torch.empty((cap,), dtype=torch.int64, device=dev)
+    o_dev = h.opts(input_on_device=True, pairs="device", pair_capacity=cap, pair_buffer=pbuf.data_ptr())
+
+    def step(opts):
+        return h.to_result(h.selfjoin_raw(xt.data_ptr(), n, d, dt, wl.k, wl.eps, opts))
+
+    for _ in range(args.warmup):
+        step(o_dev)
+    barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    results = []
+    e0.record(stream)
+    for _ in range(args.steps):
+        results.append(step(o_dev))
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    r = results[-1]
+    assert all(q.pairs_ij == r.pairs_ij for q in results)
+    join_ms = statistics.mean(q.ms["join"] for q in results)
+    launches = sum(q.kernel_launches for q in results)
+
+    # ---- e2e: host input, host pair list, through the same C ABI call
+    o_host = h.opts(pairs="host")
+    for _ in range(1):
+        h.to_result(h.selfjoin_raw(x.ctypes.data, n, d, dt, wl.k, wl.eps, o_host))
+    barrier()
+    t0 = time.perf_counter()
+    e2e_res = []
+    for _ in range(args.steps):
+        raw = h.selfjoin_raw(x.ctypes.data, n, d, dt, wl.k, wl.eps, o_host)
+        e2e_res.append((raw.pairs_ij, raw.ms_h2d, raw.ms_d2h))
+        h.lib.mistic_result_free(ctypes.byref(raw))
+    barrier()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+
+    # ---- plain FP64 CUDA-core join on the same inputs, identical pair set
+    fp64 = None
+    if not args.no_fp64:
+        pb2 = torch.empty_like(pbuf)
+        o_s = h.opts(input_on_device=True, pairs="device", pair_capacity=cap, pair_buffer=pbuf.data_ptr(),
+                     sort_pairs=True)
+        o_f = h.opts(input_on_device=True, pairs="device", pair_capacity=cap, pair_buffer=pb2.data_ptr(),
+                     sort_pairs=True, mode="fp64")
+        rs = step(o_s)
+        barrier()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        rf = step(o_f)
+        f1.record(stream)
+        barrier()
+        fms = f0.elapsed_time(f1)
+        same = (rs.pairs_ij == rf.pairs_ij and
+                bool(torch.equal(pbuf[:rs.pairs_ij], pb2[:rf.pairs_ij])))
+        fp64 = {"ms_per_step": fms, "join_ms": rf.ms["join"], "pairs_ij": rf.pairs_ij,
+                "identical_pair_set": same, "mixed_speedup": fms / ms,
+                "ulp_ambiguous": rf.ulp_ambiguous}
+
+    if rank != 0:
+        return
+    peaks = load_peaks()
+    fp32_peak = measure_fp32_peak()
+    # dominant kernel: the FP32 filter join; algorithmic work 3d flops per
+    # candidate pair (d subtractions, d multiply-adds), CUDA-core FP32 pipe.
+    flops = r.candidates * 3.0 * d
+    achieved = flops / (join_ms * 1e-3) / 1e12
+    cpu = cpu_sample(x, wl.eps, args.cpu_seconds) if not args.no_cpu else None
+    value = world * n / (ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "n": n, "d": d, "k": wl.k, "eps_hex": float(wl.eps).hex(),
+                   "desc": WORKLOADS[args.workload][1], "mode": r.mode_used,
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": f"inputs larger than L2 ({n * d * 8 / 1e6:.0f} MB points per step)",
+                   "pairs_to": "caller device buffer"},
+        "pairs_ij": r.pairs_ij, "pairs_ordered_incl_self": r.pairs_ordered_incl_self,
+        "candidates": r.candidates, "band_pairs": r.band_pairs, "ulp_ambiguous": r.ulp_ambiguous,
+        "band_fraction": r.band_pairs / max(1, r.candidates),
+        "distance_evals_per_s": r.candidates / (ms * 1e-3), "pairs_per_s": r.pairs_ij / (ms * 1e-3),
+        "phase_ms": {k: round(v, 3) for k, v in r.ms.items()},
+        "bins": r.n_bins, "bin_pairs": r.n_bin_pairs, "units": r.n_units, "k_used": r.k_used,
+        "fp64_plain": fp64,
+        "roofline": {"bound": "fp32", "kernel": "k_join_f32", "achieved": achieved,
+                     "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None,
+                     "traffic": None, "work": "3*d FP32 flops per candidate pair",
+                     "peak_source": "mistic_peaks FFMA probe, this run (CUDA-core FP32 pipe)",
+                     "hbm_peak_gbs": peaks.get("hbm_gbs"), "hbm_peak_source": peaks["_source"]},
+        "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": n * d * x.itemsize, "d2h_bytes_per_step": int(r.pairs_ij) * 8,
+                "h2d_ms": statistics.mean(t[1] for t in e2e_res), "d2h_ms": statistics.mean(t[2] for t in e2e_res)},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "cpu_baseline": None if cpu is None else {
+            "value": cpu["points_per_s"], "unit": UNIT, "cores": cpu["threads"], "kind": "port",
+            "sample": f"rows [0,{cpu['rows']}) x all {n} rows ({cpu['seconds']:.1f} s), extrapolated to "
+                      f"n rows; brute_force of src/utils.cu:285-317 (oracle C port, OpenMP)",
+            "evals_per_s": cpu["evals_per_s"]},
+    }
+    print(json.dumps(line), flush=True)
+    h.close()
+
+
+_FP32_PEAK = None
+
+
+def measure_fp32_peak() -> float | None:
+    """CUDA-core FP32 FFMA peak of this GPU from the mistic_peaks probe."""
+    global _FP32_PEAK
+    if _FP32_PEAK is not None:
+        return _FP32_PEAK
+    from mistic import build as B
+    try:
+        out = subprocess.run([B.PEAKS], capture_output=True, text=True, timeout=120).stdout
+        _FP32_PEAK = float(json.loads(out.strip().splitlines()[-1])["fp32_tflops"])
+    except Exception:
+        _FP32_PEAK = None
+    return _FP32_PEAK
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["mistic", "reference"], default="mistic")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="susy18")
+    ap.add_argument("--n", type=int, default=0, help="override the point count (testing)")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-seconds", type=float, default=6.0)
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload][0](args.n)
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_mistic(args, wl)
+
+
+if __name__ == "__main__":
+    main()

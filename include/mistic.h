@@ -1,0 +1,187 @@
+/*
+ * mistic.h — C ABI of the GB300 ε-self-join library (libmistic.so).
+ *
+ * The reference (bwd29/self-join-MiSTIC) exposes its self-join only as a
+ * command line, `build/main <file.bin> <dim> <numRP> <epsilon>`
+ * (src/main.cu:20-50), over an internal C++ entry point
+ *
+ *   struct neighborTable* nodeLauncher5(double* data, unsigned dim,
+ *       unsigned numPoints, unsigned numRP, unsigned* pointArray,
+ *       double epsilon);                               (include/launcher.cuh:77-82)
+ *
+ * that builds the index (src/nodes.cu:5-356), runs the batched distance
+ * kernel (src/kernel.cu:992-1046, launched at src/launcher.cu:3430), prints
+ * "Total results Set Size: N" with N = ordered pairs including self pairs
+ * (src/launcher.cu:3508-3515) and returns a per-point neighbour table
+ * (include/utils.cuh:33-41).  The entry points below replace that function
+ * and the CLI's data path: points, dimensionality d, reference-point count k
+ * and ε go in; the pair count (both the reference's ordered-with-self number
+ * and the unordered i<j count) and optionally the pair list come out.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only; no C++ or torch types cross this line.
+ *  - Every function returns a mistic_status; nothing aborts or hangs.  A
+ *    failing call leaves a message retrievable with mistic_last_error().
+ *  - One handle owns one CUDA stream and its cached device buffers; calls on
+ *    one handle must not overlap.  Different handles may be used from
+ *    different host threads.
+ *  - The caller owns the input; the library owns result buffers until
+ *    mistic_result_free().
+ *  - Row ids in pair lists are the caller's original row indices.
+ *
+ * The predicate is the reference's FP64 one (src/utils.cu:296-309 and
+ * src/kernel.cu:833-865): s = Σ_k (x_k - y_k)^2 summed sequentially in column
+ * order with each operation rounded, and a pair is in the result iff
+ * s <= fl(ε*ε).  Every mode returns exactly that pair set: the reduced-
+ * precision modes only pre-filter, and re-decide in FP64 every pair whose
+ * fast distance lies inside a rigorous error band around ε².
+ */
+#ifndef MISTIC_H
+#define MISTIC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MISTIC_ABI_VERSION 1
+
+typedef enum mistic_status {
+  MISTIC_OK = 0,
+  MISTIC_ERR_INVALID_ARG = 1,   /* null pointer, d == 0, eps < 0 or not finite, ... */
+  MISTIC_ERR_CUDA = 2,          /* a CUDA runtime call failed (see mistic_last_error) */
+  MISTIC_ERR_OUT_OF_MEMORY = 3, /* device or pinned host allocation failed */
+  MISTIC_ERR_TOO_LARGE = 4,     /* n >= 2^32 or d above the supported maximum */
+  MISTIC_ERR_NOT_FINITE = 5,    /* an input coordinate is NaN or infinite */
+  MISTIC_ERR_PAIR_OVERFLOW = 6, /* caller-sized pair buffer too small; counts are valid */
+  MISTIC_ERR_TIMEOUT = 7,       /* a bounded device wait gave up; the context stays usable */
+  MISTIC_ERR_NO_DEVICE = 8,     /* no CUDA device, or the device is not sm_103 */
+  MISTIC_ERR_IO = 9,            /* file could not be read */
+  MISTIC_ERR_INTERNAL = 10      /* device-side consistency check failed */
+} mistic_status;
+
+typedef enum mistic_dtype {
+  MISTIC_F64 = 0, /* row-major n x d double (the reference's only format) */
+  MISTIC_F32 = 1  /* row-major n x d float; widened exactly to FP64 for the predicate */
+} mistic_dtype;
+
+typedef enum mistic_mode {
+  MISTIC_MODE_AUTO = 0, /* the fastest exact mode for d (currently FP32 filter) */
+  MISTIC_MODE_FP64 = 1, /* plain FP64 CUDA-core distances for every candidate */
+  MISTIC_MODE_FP32 = 2  /* FP32 CUDA-core filter + FP64 re-decision of the band */
+} mistic_mode;
+
+typedef enum mistic_rp_mode {
+  MISTIC_RP_PCA = 0,  /* k far points along the sample's top-k principal axes (default) */
+  MISTIC_RP_BOX = 1,  /* k points uniform in the bounding box (seeded) */
+  MISTIC_RP_USER = 2  /* caller-supplied k x d FP64 points in opts.rp_user */
+} mistic_rp_mode;
+
+typedef enum mistic_pairs_where {
+  MISTIC_PAIRS_NONE = 0,   /* counts only; no pair list is materialised */
+  MISTIC_PAIRS_HOST = 1,   /* result.pairs is a host array owned by the result */
+  MISTIC_PAIRS_DEVICE = 2  /* result.pairs is a device array owned by the result */
+} mistic_pairs_where;
+
+typedef struct mistic_opts {
+  uint32_t struct_size;       /* = sizeof(mistic_opts); set by mistic_opts_init */
+  mistic_mode mode;
+  mistic_rp_mode rp_mode;
+  const double* rp_user;      /* k x d host array when rp_mode == MISTIC_RP_USER */
+  uint64_t seed;              /* seed for MISTIC_RP_BOX and PCA sampling */
+  int32_t input_on_device;    /* 1: pts is a device pointer on the handle's device */
+  mistic_pairs_where pairs;   /* where the pair list goes */
+  int32_t sort_pairs;         /* 1: pair list sorted ascending by (i, j) */
+  uint64_t pair_capacity;     /* 0: the library sizes the pair buffer itself */
+  uint32_t* pair_buffer;      /* MISTIC_PAIRS_DEVICE only: caller-owned device buffer of
+                                 pair_capacity pairs (2*pair_capacity uint32, 8-byte aligned),
+                                 reused across calls like the reference's preallocated
+                                 result arrays (src/launcher.cu:3340-3349); NULL: the
+                                 library allocates and the result owns the list */
+  int32_t check_finite;       /* 1 (default): reject NaN/inf inputs with MISTIC_ERR_NOT_FINITE */
+  int32_t timing;             /* 1 (default): fill the per-phase times */
+} mistic_opts;
+
+typedef struct mistic_result {
+  uint64_t n;                       /* points joined */
+  uint32_t d, k_used;               /* k_used <= k: RPs that fit the 64-bit bin key */
+  uint64_t pairs_ij;                /* unordered pairs i<j with s <= ε² */
+  uint64_t pairs_ordered_incl_self; /* 2*pairs_ij + n: the reference's "Total results Set Size" */
+  uint64_t candidates;              /* unordered candidate pairs the join evaluated */
+  uint64_t band_pairs;              /* candidates re-decided in FP64 (0 in FP64 mode) */
+  uint64_t ulp_ambiguous;           /* FP64-decided pairs with |s - ε²| <= 4 ulp(ε²) */
+  uint64_t n_bins;                  /* non-empty bins of the reference-point index */
+  uint64_t n_bin_pairs;             /* (home bin, neighbour bin) work items, home <= neighbour */
+  uint64_t n_units;                 /* join work units after splitting */
+  uint32_t* pairs;                  /* 2*pairs_ij uint32 (i, j), i < j, or NULL */
+  uint64_t pairs_len;               /* pairs stored (== pairs_ij unless capped) */
+  int32_t pairs_on_device;
+  mistic_mode mode_used;
+  /* per-phase device times (CUDA events on the handle's stream), ms */
+  double ms_total, ms_h2d, ms_prep, ms_keys, ms_sort, ms_bins, ms_enum, ms_join, ms_d2h;
+  double ms_wall;                   /* host wall time of the whole call */
+  uint32_t kernel_launches;         /* library kernels launched by this call */
+  void* _owner;                     /* internal: non-NULL when the result owns `pairs` */
+} mistic_result;
+
+typedef struct mistic_instance {   /* one self-join of a batch */
+  const void* pts;
+  uint64_t n;
+  uint32_t d;
+  mistic_dtype dtype;
+  uint32_t k;
+  double eps;
+} mistic_instance;
+
+typedef struct mistic_handle_s* mistic_handle;
+
+/* Library/ABI version; lets a binding check it loaded a compatible build. */
+int mistic_abi_version(void);
+
+/* Fill opts with defaults (AUTO mode, PCA reference points, counts only). */
+void mistic_opts_init(mistic_opts* opts);
+
+/* Create a handle on `device`.  `stream` is a cudaStream_t to run on, or NULL
+ * for a stream owned by the handle.  Replaces the reference's
+ * cudaSetDevice(CUDA_DEVICE) + per-call allocations (src/main.cu:22,
+ * src/launcher.cu:3259-3349). */
+mistic_status mistic_create(mistic_handle* out, int device, void* stream);
+mistic_status mistic_destroy(mistic_handle h);
+
+/* The ε-self-join of n points (replaces nodeLauncher5, include/launcher.cuh:77-82,
+ * and the join path of main, src/main.cu:20-182).  k is the number of
+ * reference points of the bin index (the reference parses numRP at
+ * src/main.cu:27 but always builds MAXRP = 6 layers, src/nodes.cu:62).
+ * n == 0 and n == 1 are valid and yield zero pairs. */
+mistic_status mistic_selfjoin(mistic_handle h, const void* pts, uint64_t n,
+                              uint32_t d, mistic_dtype dtype, uint32_t k,
+                              double eps, const mistic_opts* opts,
+                              mistic_result* result);
+
+/* m independent self-joins on one handle; results[i] receives instance i.
+ * The reference has no batch entry point (one process per dataset,
+ * script.sh:86-117); this replaces that loop. */
+mistic_status mistic_batch_selfjoin(mistic_handle h, const mistic_instance* inst,
+                                    uint32_t m, const mistic_opts* opts,
+                                    mistic_result* results);
+
+/* Read a raw little-endian row-major point file (the reference's input
+ * format, src/main.cu:42-50: n = bytes / sizeof(elem) / d) into a malloc'd
+ * host array released with mistic_free_host. */
+mistic_status mistic_read_points(const char* path, uint32_t d, mistic_dtype dtype,
+                                 void** out_pts, uint64_t* out_n);
+void mistic_free_host(void* p);
+
+/* Release the buffers a result owns (pair list).  Safe on a zeroed result. */
+void mistic_result_free(mistic_result* r);
+
+const char* mistic_strerror(mistic_status s);
+const char* mistic_last_error(mistic_handle h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MISTIC_H */

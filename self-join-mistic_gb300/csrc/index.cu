@@ -1,0 +1,505 @@
+// Reference-point bin index and neighbour-bin enumeration on the device.
+//
+// Reference counterparts (bwd29/self-join-MiSTIC):
+//  - binningKernel, src/kernel.cu:880-909: per point, floor(||x - r|| / ε)
+//    for each reference point in FP64.  Here the same FP64 distances are
+//    taken to k reference points and quantised with a width slightly above ε
+//    so the triangle-inequality argument survives rounding (see k_pack_keys).
+//  - the host-built node net, src/nodes.cu:5-356, whose neighbour relation is
+//    "bins differ by at most one on every layer" (src/nodes.cu:416-435,
+//    719-747).  Here the bin keys are packed into one 64-bit key, radix
+//    sorted, and non-empty bins become contiguous runs of the sorted order.
+//  - the 3^k neighbour search over sorted bin keys, generateRanges /
+//    binarySearch in src/tree.cu:596-759,886-996 (device form
+//    GPUBinarySearch, src/kernel.cu:164-224).  Here one thread per non-empty
+//    bin walks the ±1 neighbourhood depth-first, narrowing a sorted range one
+//    key field at a time, so empty prefixes are pruned early; only
+//    neighbours of index >= the home bin are emitted (each unordered bin pair
+//    once).
+#include <math.h>
+
+#include "internal.cuh"
+
+namespace mistic {
+
+template <class T>
+__device__ __forceinline__ double ld(const T* p, size_t i) {
+  return (double)p[i];
+}
+
+// ------------------------------------------------------------ column stats
+// Per-column min, max and sum over all rows plus a finiteness flag.  Each
+// block writes its partials; a second kernel folds them in a fixed order so
+// the result (and therefore the reference points) is deterministic.
+
+constexpr int CS_ROWS = 8;
+
+template <class T>
+__global__ void k_colstats(const T* __restrict__ x, size_t n, uint32_t d, double* __restrict__ part,
+                           unsigned* __restrict__ nonfinite) {
+  // part layout: [blockIdx.y][3][d] : min, max, sum for the block's rows of column tile blockIdx.x
+  __shared__ double smin[CS_ROWS][32], smax[CS_ROWS][32], ssum[CS_ROWS][32];
+  const uint32_t col = blockIdx.x * 32 + threadIdx.x;
+  double mn = INFINITY, mx = -INFINITY, sm = 0.0;
+  bool bad = false;
+  if (col < d) {
+    for (size_t r = (size_t)blockIdx.y * CS_ROWS + threadIdx.y; r < n; r += (size_t)gridDim.y * CS_ROWS) {
+      double v = ld(x, r * d + col);
+      if (!isfinite(v)) bad = true;
+      mn = fmin(mn, v);
+      mx = fmax(mx, v);
+      sm += v;
+    }
+  }
+  if (bad) atomicOr(nonfinite, 1u);
+  smin[threadIdx.y][threadIdx.x] = mn;
+  smax[threadIdx.y][threadIdx.x] = mx;
+  ssum[threadIdx.y][threadIdx.x] = sm;
+  __syncthreads();
+  if (threadIdx.y == 0 && col < d) {
+    for (int r = 1; r < CS_ROWS; ++r) {
+      mn = fmin(mn, smin[r][threadIdx.x]);
+      mx = fmax(mx, smax[r][threadIdx.x]);
+      sm += ssum[r][threadIdx.x];
+    }
+    double* p = part + (size_t)blockIdx.y * 3 * d;
+    p[col] = mn;
+    p[d + col] = mx;
+    p[2 * d + col] = sm;
+  }
+}
+
+__global__ void k_colstats_final(const double* __restrict__ part, uint32_t nparts, uint32_t d,
+                                 size_t n, double* __restrict__ out /* mean, min, max */) {
+  const uint32_t col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= d) return;
+  double mn = INFINITY, mx = -INFINITY, sm = 0.0;
+  for (uint32_t b = 0; b < nparts; ++b) {
+    const double* p = part + (size_t)b * 3 * d;
+    mn = fmin(mn, p[col]);
+    mx = fmax(mx, p[d + col]);
+    sm += p[2 * d + col];
+  }
+  out[col] = n ? sm / (double)n : 0.0;
+  out[d + col] = mn;
+  out[2 * d + col] = mx;
+}
+
+// ------------------------------------------------------------ sample covariance
+template <class T>
+__global__ void k_gather_sample(const T* __restrict__ x, size_t n, uint32_t d, uint32_t S,
+                                double* __restrict__ s) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)S * d) return;
+  const size_t row = i / d, col = i % d;
+  const size_t src = (size_t)((row * (unsigned long long)n) / S);
+  s[i] = ld(x, src * d + col);
+}
+
+// cov[a][b] = mean over the sample of (s_a - mu_a)(s_b - mu_b); mu = sample mean
+__global__ void k_sample_cov(const double* __restrict__ s, uint32_t S, uint32_t d,
+                             double* __restrict__ cov) {
+  const uint32_t a = blockIdx.y * blockDim.y + threadIdx.y;
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= d || b >= d || b < a) return;
+  double ma = 0, mb = 0;
+  for (uint32_t r = 0; r < S; ++r) {
+    ma += s[(size_t)r * d + a];
+    mb += s[(size_t)r * d + b];
+  }
+  ma /= S;
+  mb /= S;
+  double c = 0;
+  for (uint32_t r = 0; r < S; ++r) c += (s[(size_t)r * d + a] - ma) * (s[(size_t)r * d + b] - mb);
+  c /= S;
+  cov[(size_t)a * d + b] = c;
+  cov[(size_t)b * d + a] = c;
+}
+
+// ------------------------------------------------------------ reference-point distances
+// D[i][j] = FP64 ||x_i - r_j|| (sequential sum, then sqrt), with per-block
+// min/max partials per reference point.
+constexpr int RPD_THREADS = 256;
+
+template <class T>
+__global__ void __launch_bounds__(RPD_THREADS)
+k_rp_dist(const T* __restrict__ x, size_t n, uint32_t d, const double* __restrict__ rps, int k,
+          double* __restrict__ D, double* __restrict__ part /* [block][2][k] */) {
+  extern __shared__ double srp[];  // k x d
+  for (uint32_t i = threadIdx.x; i < (uint32_t)k * d; i += blockDim.x) srp[i] = rps[i];
+  __shared__ double smn[MAX_K][RPD_THREADS / 32], smx[MAX_K][RPD_THREADS / 32];
+  __syncthreads();
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < n;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j = 0; j < k; ++j) {
+    double dist = 0.0;
+    if (valid) {
+      double s = 0.0;
+      const double* r = srp + (size_t)j * d;
+      for (uint32_t t = 0; t < d; ++t) {
+        double df = ld(x, i * d + t) - r[t];
+        s = fma(df, df, s);
+      }
+      dist = sqrt(s);
+      D[i * k + j] = dist;
+    }
+    double mn = valid ? dist : INFINITY, mx = valid ? dist : -INFINITY;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      mn = fmin(mn, __shfl_xor_sync(FULL_MASK, mn, o));
+      mx = fmax(mx, __shfl_xor_sync(FULL_MASK, mx, o));
+    }
+    if (lane == 0) {
+      smn[j][w] = mn;
+      smx[j][w] = mx;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < (unsigned)k) {
+    const int j = threadIdx.x;
+    double mn = INFINITY, mx = -INFINITY;
+    for (int ww = 0; ww < RPD_THREADS / 32; ++ww) {
+      mn = fmin(mn, smn[j][ww]);
+      mx = fmax(mx, smx[j][ww]);
+    }
+    part[(size_t)blockIdx.x * 2 * k + j] = mn;
+    part[(size_t)blockIdx.x * 2 * k + k + j] = mx;
+  }
+}
+
+__global__ void k_minmax_final(const double* __restrict__ part, uint32_t nparts, int k,
+                               double* __restrict__ out /* min[k], max[k] */) {
+  const int j = threadIdx.x;
+  if (j >= k) return;
+  double mn = INFINITY, mx = -INFINITY;
+  for (uint32_t b = 0; b < nparts; ++b) {
+    mn = fmin(mn, part[(size_t)b * 2 * k + j]);
+    mx = fmax(mx, part[(size_t)b * 2 * k + k + j]);
+  }
+  out[j] = mn;
+  out[k + j] = mx;
+}
+
+// ------------------------------------------------------------ key packing
+// field_j = floor((D_ij - Dmin_j) / w_j), clamped to [0, maxkey_j].
+// Completeness: for any pair in the result, |D_xj - D_yj| (computed) is
+// below w_j, so the two fields differ by at most one; w_j = ε(1+δ) with δ
+// covering the FP64 rounding of the distances and of the quotient (chosen
+// on the host).  Clamping only shrinks differences.
+__global__ void k_pack_keys(const double* __restrict__ D, size_t n, PackParams P,
+                            uint64_t* __restrict__ keys) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t key = 0;
+  for (int j = 0; j < P.k; ++j) {
+    double v = floor((D[i * P.kstride + P.col[j]] - P.dmin[j]) / P.w[j]);
+    v = fmin(fmax(v, 0.0), (double)P.maxkey[j]);
+    key |= (uint64_t)v << P.shift[j];
+  }
+  keys[i] = key;
+}
+
+__global__ void k_iota(uint32_t* v, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = (uint32_t)i;
+}
+
+// ------------------------------------------------------------ bins
+__global__ void k_bin_flags(const uint64_t* __restrict__ keys, size_t n, uint32_t* __restrict__ flags) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  flags[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+__global__ void k_bin_starts(const uint64_t* __restrict__ keys, size_t n,
+                             const uint32_t* __restrict__ binid /* exclusive scan of flags */,
+                             uint32_t* __restrict__ bstart, uint64_t* __restrict__ bkey) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bool head = (i == 0 || keys[i] != keys[i - 1]);
+  if (head) {
+    bstart[binid[i]] = (uint32_t)i;
+    bkey[binid[i]] = keys[i];
+  }
+  if (i == n - 1) bstart[binid[i] + (head ? 1 : 0)] = (uint32_t)n;
+}
+
+// ------------------------------------------------------------ point gather
+// Sorted-order copies for the join: FP32 centred coordinates (row stride
+// dpad, zero padded), the original row ids, and optionally FP64 rows for the
+// plain FP64 join.  Also the largest FP32 row norm (for the filter's error
+// bound), reduced per block.
+template <class T>
+__global__ void k_gather_points(const T* __restrict__ x, size_t n, uint32_t d,
+                                const uint32_t* __restrict__ perm, const double* __restrict__ center,
+                                uint32_t dpad32, float* __restrict__ xf, uint32_t dpad64,
+                                double* __restrict__ xd, uint32_t* __restrict__ ids,
+                                double* __restrict__ norm_part) {
+  const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double nrm2 = 0.0;
+  if (p < n) {
+    const uint32_t src = perm[p];
+    ids[p] = src;
+    for (uint32_t t = 0; t < dpad32; ++t) {
+      float v = 0.f;
+      if (t < d) v = (float)(ld(x, (size_t)src * d + t) - center[t]);
+      if (xf) xf[p * dpad32 + t] = v;
+      nrm2 = fma((double)v, (double)v, nrm2);
+    }
+    if (xd) {
+      for (uint32_t t = 0; t < dpad64; ++t) xd[p * dpad64 + t] = t < d ? ld(x, (size_t)src * d + t) : 0.0;
+    }
+  }
+  // block max of nrm2
+#pragma unroll
+  for (int o = 16; o; o >>= 1) nrm2 = fmax(nrm2, __shfl_xor_sync(FULL_MASK, nrm2, o));
+  __shared__ double sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = nrm2;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, sm[w]);
+    norm_part[blockIdx.x] = m;
+  }
+}
+
+__global__ void k_max_final(const double* __restrict__ part, uint32_t nparts, double* out) {
+  double m = 0;
+  for (uint32_t i = threadIdx.x; i < nparts; i += blockDim.x) m = fmax(m, part[i]);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(FULL_MASK, m, o));
+  __shared__ double sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, sm[w]);
+    *out = r;
+  }
+}
+
+// ------------------------------------------------------------ neighbour enumeration
+// One thread per non-empty bin h.  Depth-first over the key fields: at
+// level j the candidate field value is K_j - 1, K_j, K_j + 1; the bins whose
+// key starts with the chosen prefix form a contiguous sorted range, found by
+// two lower-bound searches inside the parent range.  A range lying wholly
+// below h is skipped (home <= neighbour).  Leaves come out in ascending bin
+// order, starting with h itself.
+//
+// Pass 1 (fill == false) counts neighbours, join work units and candidate
+// pairs per home bin; pass 2 writes the neighbour list and the units.  The
+// neighbour list of h is cut into segments of about `seg_cap` candidate
+// points, and the home bin into chunks of `chunk` points; one unit is one
+// (chunk, segment) combination.
+__device__ __forceinline__ uint32_t lower_bound_u64(const uint64_t* __restrict__ a, uint32_t lo,
+                                                    uint32_t hi, uint64_t v) {
+  while (lo < hi) {
+    uint32_t mid = lo + ((hi - lo) >> 1);
+    if (a[mid] < v)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+template <bool FILL>
+__global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __restrict__ bstart,
+                       uint32_t m, EnumParams P, uint32_t* __restrict__ nbr_cnt,
+                       uint32_t* __restrict__ unit_cnt, unsigned long long* __restrict__ cand,
+                       const uint32_t* __restrict__ nbr_off, const uint32_t* __restrict__ unit_off,
+                       uint32_t* __restrict__ nbr, Unit* __restrict__ units) {
+  const uint32_t hb = blockIdx.x * blockDim.x + threadIdx.x;
+  if (hb >= m) return;
+  const uint64_t K = bkey[hb];
+  const uint32_t asz = bstart[hb + 1] - bstart[hb];
+  const uint32_t nchunks = (asz + P.chunk - 1) / P.chunk;
+
+  int kf[MAX_K];
+  // decode fields: field j spans [shift[j], shift[j-1]) (shift[-1] = 64)
+  for (int j = 0; j < P.k; ++j) {
+    const int hi_bit = j == 0 ? 64 : P.shift[j - 1];
+    const int width = hi_bit - P.shift[j];
+    const uint64_t mask = width >= 64 ? ~0ull : ((1ull << width) - 1ull);
+    kf[j] = (int)((K >> P.shift[j]) & mask);
+  }
+
+  uint32_t lo[MAX_K + 1], hi[MAX_K + 1];
+  uint64_t base[MAX_K + 1];
+  int di[MAX_K + 1];
+  lo[0] = 0;
+  hi[0] = m;
+  base[0] = 0;
+  di[0] = 0;
+  int j = 0;
+
+  uint32_t cnt = 0, nseg = 0, seg_fill = 0, seg_begin = 0;
+  unsigned long long c = 0;
+  uint32_t w_nbr = FILL ? nbr_off[hb] : 0;
+  uint32_t w_unit = FILL ? unit_off[hb] : 0;
+
+  // Visits neighbour bin `a` (ascending, a >= hb): candidate count, segment
+  // split and, in pass 2, the neighbour list and the units.
+  auto leaf = [&](uint32_t a) {
+    const uint32_t bsz = bstart[a + 1] - bstart[a];
+    c += (a == hb) ? (unsigned long long)asz * (asz - 1) / 2 : (unsigned long long)asz * bsz;
+    if (seg_fill > 0 && seg_fill + bsz > P.seg_cap) {
+      if (FILL) {
+        for (uint32_t ch = 0; ch < nchunks; ++ch)
+          units[w_unit++] = Unit{hb, ch, nbr_off[hb] + seg_begin, nbr_off[hb] + cnt};
+      }
+      ++nseg;
+      seg_fill = 0;
+      seg_begin = cnt;
+    }
+    seg_fill += bsz;
+    if (FILL) nbr[w_nbr++] = a;
+    ++cnt;
+  };
+
+  if (P.k == 0) {
+    leaf(hb);  // no key fields: one bin holding every point
+    j = -1;
+  }
+  while (j >= 0) {
+    if (di[j] == 3) {
+      --j;
+      if (j >= 0) ++di[j];
+      continue;
+    }
+    const int cv = kf[j] + di[j] - 1;
+    if (cv < 0 || (long long)cv > (long long)P.maxkey[j]) {
+      ++di[j];
+      continue;
+    }
+    const uint64_t lower = base[j] | ((uint64_t)cv << P.shift[j]);
+    const uint64_t upper = lower + (1ull << P.shift[j]);
+    const uint32_t a = lower_bound_u64(bkey, lo[j], hi[j], lower);
+    const uint32_t b = lower_bound_u64(bkey, a, hi[j], upper);
+    if (a == b || b <= hb) {
+      ++di[j];
+      continue;
+    }
+    if (j == P.k - 1) {
+      leaf(a);  // b == a + 1 and a >= hb
+      ++di[j];
+      continue;
+    }
+    base[j + 1] = lower;
+    lo[j + 1] = a;
+    hi[j + 1] = b;
+    di[j + 1] = 0;
+    ++j;
+  }
+  if (cnt > 0) {
+    if (FILL) {
+      for (uint32_t ch = 0; ch < nchunks; ++ch)
+        units[w_unit++] = Unit{hb, ch, nbr_off[hb] + seg_begin, nbr_off[hb] + cnt};
+    }
+    ++nseg;
+  }
+  if (!FILL) {
+    nbr_cnt[hb] = cnt;
+    unit_cnt[hb] = nseg * nchunks;
+    cand[hb] = c;
+  }
+}
+
+// ------------------------------------------------------------ host launchers
+namespace idx {
+
+void colstats(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, uint32_t d,
+              double* part, uint32_t nparts, double* out, unsigned* nonfinite) {
+  dim3 blk(32, CS_ROWS), grd((d + 31) / 32, nparts);
+  if (dt == MISTIC_F64)
+    k_colstats<double><<<grd, blk, 0, h->stream>>>((const double*)x, n, d, part, nonfinite);
+  else
+    k_colstats<float><<<grd, blk, 0, h->stream>>>((const float*)x, n, d, part, nonfinite);
+  launched(h, "colstats");
+  k_colstats_final<<<(d + 127) / 128, 128, 0, h->stream>>>(part, nparts, d, n, out);
+  launched(h, "colstats_final");
+}
+
+void sample_cov(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, uint32_t d,
+                uint32_t S, double* sbuf, double* cov) {
+  const size_t tot = (size_t)S * d;
+  const unsigned nb = (unsigned)((tot + 255) / 256);
+  if (dt == MISTIC_F64)
+    k_gather_sample<double><<<nb, 256, 0, h->stream>>>((const double*)x, n, d, S, sbuf);
+  else
+    k_gather_sample<float><<<nb, 256, 0, h->stream>>>((const float*)x, n, d, S, sbuf);
+  launched(h, "gather_sample");
+  dim3 blk(16, 16), grd((d + 15) / 16, (d + 15) / 16);
+  k_sample_cov<<<grd, blk, 0, h->stream>>>(sbuf, S, d, cov);
+  launched(h, "sample_cov");
+}
+
+void rp_dist(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, uint32_t d,
+             const double* rps, int k, double* D, double* part, uint32_t nparts, double* mm) {
+  const size_t smem = (size_t)k * d * sizeof(double);
+  if (smem > 48 * 1024) {
+    if (dt == MISTIC_F64)
+      MCK(cudaFuncSetAttribute(k_rp_dist<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    else
+      MCK(cudaFuncSetAttribute(k_rp_dist<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
+  if (dt == MISTIC_F64)
+    k_rp_dist<double><<<nparts, RPD_THREADS, smem, h->stream>>>((const double*)x, n, d, rps, k, D, part);
+  else
+    k_rp_dist<float><<<nparts, RPD_THREADS, smem, h->stream>>>((const float*)x, n, d, rps, k, D, part);
+  launched(h, "rp_dist");
+  k_minmax_final<<<1, 32, 0, h->stream>>>(part, nparts, k, mm);
+  launched(h, "minmax_final");
+}
+
+void pack_keys(mistic_handle_s* h, const double* D, size_t n, const PackParams& P, uint64_t* keys) {
+  k_pack_keys<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(D, n, P, keys);
+  launched(h, "pack_keys");
+}
+
+void iota(mistic_handle_s* h, uint32_t* v, size_t n) {
+  k_iota<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(v, n);
+  launched(h, "iota");
+}
+
+void bins(mistic_handle_s* h, const uint64_t* keys, size_t n, uint32_t* flags, uint32_t* nbins_dev,
+          uint32_t* bstart, uint64_t* bkey) {
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  k_bin_flags<<<nb, 256, 0, h->stream>>>(keys, n, flags);
+  launched(h, "bin_flags");
+  exclusive_scan<uint32_t>(h, flags, flags, n, nbins_dev);
+  k_bin_starts<<<nb, 256, 0, h->stream>>>(keys, n, flags, bstart, bkey);
+  launched(h, "bin_starts");
+}
+
+void gather(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, uint32_t d,
+            const uint32_t* perm, const double* center, uint32_t dpad32, float* xf, uint32_t dpad64,
+            double* xd, uint32_t* ids, double* norm_part, double* rmax) {
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  if (dt == MISTIC_F64)
+    k_gather_points<double><<<nb, 256, 0, h->stream>>>((const double*)x, n, d, perm, center, dpad32, xf,
+                                                      dpad64, xd, ids, norm_part);
+  else
+    k_gather_points<float><<<nb, 256, 0, h->stream>>>((const float*)x, n, d, perm, center, dpad32, xf,
+                                                     dpad64, xd, ids, norm_part);
+  launched(h, "gather_points");
+  k_max_final<<<1, 1024, 0, h->stream>>>(norm_part, nb, rmax);
+  launched(h, "max_final");
+}
+
+void enumerate(mistic_handle_s* h, const uint64_t* bkey, const uint32_t* bstart, uint32_t m,
+               const EnumParams& P, uint32_t* nbr_cnt, uint32_t* unit_cnt, unsigned long long* cand,
+               const uint32_t* nbr_off, const uint32_t* unit_off, uint32_t* nbr, Unit* units, bool fill) {
+  const unsigned nb = (m + 127) / 128;
+  if (!fill)
+    k_enum<false><<<nb, 128, 0, h->stream>>>(bkey, bstart, m, P, nbr_cnt, unit_cnt, cand, nullptr, nullptr,
+                                             nullptr, nullptr);
+  else
+    k_enum<true><<<nb, 128, 0, h->stream>>>(bkey, bstart, m, P, nullptr, nullptr, nullptr, nbr_off, unit_off,
+                                            nbr, units);
+  launched(h, fill ? "enum_fill" : "enum_count");
+}
+
+}  // namespace idx
+}  // namespace mistic

@@ -1,0 +1,192 @@
+// Internal declarations shared by the libmistic translation units.
+// Nothing here crosses the C ABI (include/mistic.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mistic.h"
+
+namespace mistic {
+
+constexpr unsigned FULL_MASK = 0xffffffffu;
+constexpr int MAX_K = 16;        // reference points per bin key
+constexpr int KEY_BITS_MAX = 63; // packed key budget (one spare bit keeps range ends in u64)
+constexpr uint32_t MAX_D = 4096; // dimensionality limit of the join kernels
+
+// Error carried from deep inside the pipeline to the C ABI boundary, where it
+// becomes a mistic_status plus the handle's last-error text.
+struct Error : std::runtime_error {
+  mistic_status status;
+  Error(mistic_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+[[noreturn]] void throw_cuda(cudaError_t e, const char* what, const char* file, int line);
+
+#define MCK(call)                                                   \
+  do {                                                              \
+    cudaError_t e__ = (call);                                       \
+    if (e__ != cudaSuccess) ::mistic::throw_cuda(e__, #call, __FILE__, __LINE__); \
+  } while (0)
+
+// Device buffers owned by a handle, grown on demand and reused across calls
+// (the reference allocates everything per call, src/launcher.cu:3259-3349).
+struct Arena {
+  struct Buf {
+    void* p = nullptr;
+    size_t bytes = 0;
+  };
+  std::map<std::string, Buf> bufs;
+  cudaStream_t stream = nullptr;  // work using the buffers; drained before a regrow
+  void* get(const std::string& name, size_t bytes);
+  void release_all();
+};
+
+// Key layout of the packed bin key: reference point j occupies `bits[j]`
+// bits at `shift[j]`; reference point 0 is the most significant field, so
+// numeric order of the packed key is lexicographic order of the key vector.
+struct KeyLayout {
+  int k;
+  int total_bits;
+  int bits[MAX_K];
+  int shift[MAX_K];
+  int32_t minkey[MAX_K];  // subtracted before packing
+  uint32_t maxkey[MAX_K]; // largest stored field value (after subtraction)
+};
+
+// One join work unit: a chunk of up to `CH` points of home bin `h` against
+// the neighbour bins nbr[s0 .. s1) (all of index >= h).
+struct Unit {
+  uint32_t h;
+  uint32_t chunk;
+  uint32_t s0;
+  uint32_t s1;
+};
+
+// Counters the join kernels accumulate on the device.
+struct JoinCounters {
+  unsigned long long pairs;      // accepted unordered pairs
+  unsigned long long band;       // pairs re-decided in FP64
+  unsigned long long ambiguous;  // FP64 value within 4 ulp of eps2
+  unsigned long long next_unit;  // work-queue cursor
+};
+
+// Key packing: field f = floor((D[i*kstride + col[f]] - dmin[f]) / w[f]),
+// clamped to [0, maxkey[f]], stored at bit `shift[f]`.
+struct PackParams {
+  int k;
+  int kstride;
+  int col[MAX_K];
+  double dmin[MAX_K];
+  double w[MAX_K];
+  uint32_t maxkey[MAX_K];
+  int shift[MAX_K];
+};
+
+// Neighbour enumeration: the same field layout, plus the unit split sizes.
+struct EnumParams {
+  int k;
+  int shift[MAX_K];
+  uint32_t maxkey[MAX_K];
+  uint32_t seg_cap;  // candidate points per neighbour segment
+  uint32_t chunk;    // home points per unit
+};
+
+struct JoinParams {
+  const Unit* units;
+  unsigned long long n_units;
+  const uint32_t* bstart;
+  const uint32_t* nbr;
+  const uint32_t* ids;
+  const void* xs;       // sorted rows: float (FP32 mode) or double (FP64 mode), stride dpad
+  uint32_t dpad;
+  const void* raw;      // caller's rows (device), indexed by original id, for FP64 re-decision
+  int raw_f32;
+  uint32_t d;
+  float t_lo, t_hi;     // FP32 mode: accept at or below t_lo, re-decide in (t_lo, t_hi]
+  double eps2;          // fl(ε*ε)
+  double amb;           // 4 ulp(eps2)
+  unsigned long long* pairs;  // packed (i << 32 | j), i < j; null when counting only
+  unsigned long long cap;
+  JoinCounters* ctr;
+};
+
+struct Timer {
+  cudaEvent_t ev[24];
+  int used = 0;
+};
+
+}  // namespace mistic
+
+struct mistic_handle_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int sms = 0;
+  std::string last_error;
+  mistic::Arena arena;
+  void* pinned = nullptr;  // small pinned block for scalar read-backs
+  size_t pinned_bytes = 0;
+  cudaEvent_t ev[16] = {};
+  uint32_t launches = 0;
+};
+
+namespace mistic {
+
+// Records a kernel launch for the result's kernel_launches counter and
+// checks the launch status.
+void launched(mistic_handle_s* h, const char* what);
+
+// ---- scan.cu
+template <class T>
+void exclusive_scan(mistic_handle_s* h, const T* in, T* out, size_t n, T* total_dev);
+size_t scan_partials_count(size_t n);
+
+// ---- sort.cu: LSD radix sort of 64-bit keys over the low `bits` bits with
+// an optional 32-bit payload.  If vals_in is null the payload is the input
+// position.  Returns which buffer (0/1) holds the result.
+int radix_sort_u64(mistic_handle_s* h, uint64_t* keys[2], uint32_t* vals[2],
+                   bool has_vals, bool iota_vals, size_t n, int bits);
+
+// ---- index.cu
+namespace idx {
+void colstats(mistic_handle_s*, const void* x, mistic_dtype, size_t n, uint32_t d, double* part,
+              uint32_t nparts, double* out, unsigned* nonfinite);
+void sample_cov(mistic_handle_s*, const void* x, mistic_dtype, size_t n, uint32_t d, uint32_t S,
+                double* sbuf, double* cov);
+void rp_dist(mistic_handle_s*, const void* x, mistic_dtype, size_t n, uint32_t d, const double* rps,
+             int k, double* D, double* part, uint32_t nparts, double* mm);
+void pack_keys(mistic_handle_s*, const double* D, size_t n, const PackParams&, uint64_t* keys);
+void iota(mistic_handle_s*, uint32_t* v, size_t n);
+void bins(mistic_handle_s*, const uint64_t* keys, size_t n, uint32_t* flags, uint32_t* nbins_dev,
+          uint32_t* bstart, uint64_t* bkey);
+void gather(mistic_handle_s*, const void* x, mistic_dtype, size_t n, uint32_t d, const uint32_t* perm,
+            const double* center, uint32_t dpad32, float* xf, uint32_t dpad64, double* xd,
+            uint32_t* ids, double* norm_part, double* rmax);
+void enumerate(mistic_handle_s*, const uint64_t* bkey, const uint32_t* bstart, uint32_t m,
+               const EnumParams&, uint32_t* nbr_cnt, uint32_t* unit_cnt, unsigned long long* cand,
+               const uint32_t* nbr_off, const uint32_t* unit_off, uint32_t* nbr, Unit* units,
+               bool fill);
+}  // namespace idx
+
+// ---- join.cu
+namespace join {
+int chunk_for(bool fp64, uint32_t dpad);
+void run(mistic_handle_s*, bool fp64, int CH, const JoinParams&);
+}  // namespace join
+
+// ---- rp.cpp: reference-point selection on the host.
+// stats: per-dim mean (d), min (d), max (d); cov: d x d sample covariance.
+void select_reference_points(const mistic_opts& o, uint32_t d, uint32_t k,
+                             const std::vector<double>& mean,
+                             const std::vector<double>& mn,
+                             const std::vector<double>& mx,
+                             const std::vector<double>& cov,
+                             std::vector<double>& rps);
+
+}  // namespace mistic

@@ -1,0 +1,299 @@
+// Distance join over the bin index, with result-pair compaction.
+//
+// Reference counterpart: nodeByPoint5 + cachedDistanceCheck,
+// src/kernel.cu:992-1046 and :833-865 (launched per batch at
+// src/launcher.cu:3430).  There, `tpp` threads share one query point, loop
+// over the neighbour nodes' points, test Σ(p - q)^2 <= ε² in FP64 and append
+// every hit with a global 64-bit atomicAdd into two 2.5e9-entry arrays.
+//
+// Here:
+//  - Work is a device list of units (a chunk of up to CH points of a home
+//    bin against a segment of its neighbour-bin list, neighbours >= home),
+//    drained by persistent warps through an atomic cursor, so skewed bins
+//    spread over all SMs.
+//  - The home chunk is staged in shared memory; each lane holds one
+//    candidate row in registers and accumulates CH distances at once, so a
+//    shared-memory broadcast load feeds 4 dimensions of one distance.
+//  - FP32 mode filters with FP32 distances on centred coordinates and sends
+//    only pairs whose FP32 value lies within a rigorous error band of ε² to
+//    an FP64 re-decision with the reference predicate; FP64 mode evaluates
+//    the reference predicate for every candidate.
+//  - A warp votes first; only warps holding a hit or a band pair take the
+//    slow path, where hits are counted with one warp scan and one atomicAdd.
+#include <math.h>
+
+#include <algorithm>
+
+#include "internal.cuh"
+
+namespace mistic {
+
+constexpr int JOIN_THREADS = 256;
+
+__device__ __forceinline__ uint32_t warp_incl_scan_u32(uint32_t x) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(FULL_MASK, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
+// The reference predicate (src/utils.cu:296-309): sequential, each of the
+// subtraction, product and sum rounded to FP64 (no contraction).
+__device__ __forceinline__ double exact_sqdist(const JoinParams& P, uint32_t i, uint32_t j) {
+  double s = 0.0;
+  if (P.raw_f32) {
+    const float* a = (const float*)P.raw + (size_t)i * P.d;
+    const float* b = (const float*)P.raw + (size_t)j * P.d;
+    for (uint32_t t = 0; t < P.d; ++t) {
+      double df = __dsub_rn((double)a[t], (double)b[t]);
+      s = __dadd_rn(s, __dmul_rn(df, df));
+    }
+  } else {
+    const double* a = (const double*)P.raw + (size_t)i * P.d;
+    const double* b = (const double*)P.raw + (size_t)j * P.d;
+    for (uint32_t t = 0; t < P.d; ++t) {
+      double df = __dsub_rn(a[t], b[t]);
+      s = __dadd_rn(s, __dmul_rn(df, df));
+    }
+  }
+  return s;
+}
+
+// Emits the accepted pairs of one lane (bit a of `acc` = home point a0 + a
+// paired with candidate q), one atomicAdd per warp.
+__device__ __forceinline__ void emit_pairs(const JoinParams& P, uint32_t acc, uint32_t a0, uint32_t q) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t cnt = __popc(acc);
+  const uint32_t incl = warp_incl_scan_u32(cnt);
+  const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+  if (total == 0) return;
+  unsigned long long base = 0;
+  if (lane == 31) base = atomicAdd(&P.ctr->pairs, (unsigned long long)total);
+  base = __shfl_sync(FULL_MASK, base, 31);
+  if (P.pairs && cnt) {
+    unsigned long long pos = base + incl - cnt;
+    const uint32_t iq = P.ids[q];
+    while (acc) {
+      const int a = __ffs(acc) - 1;
+      acc &= acc - 1;
+      const uint32_t ia = P.ids[a0 + a];
+      const uint32_t lo = ia < iq ? ia : iq, hi = ia < iq ? iq : ia;
+      if (pos < P.cap) P.pairs[pos] = ((unsigned long long)lo << 32) | hi;
+      ++pos;
+    }
+  }
+}
+
+__device__ __forceinline__ void add_counter(unsigned long long* c, uint32_t v) {
+  const int lane = threadIdx.x & 31;
+  uint32_t s = warp_incl_scan_u32(v);
+  s = __shfl_sync(FULL_MASK, s, 31);
+  if (lane == 0 && s) atomicAdd(c, (unsigned long long)s);
+}
+
+// Valid-home mask for candidate q: home points a0 .. a0+na-1, and in the
+// home bin itself only pairs with sorted position a < q.
+__device__ __forceinline__ uint32_t home_mask(uint32_t na, bool self, uint32_t q, uint32_t a0, int CH) {
+  uint32_t m = na >= 32 ? FULL_MASK : ((1u << na) - 1u);
+  if (self) {
+    const int lim = (int)q - (int)a0;
+    m &= lim >= 32 ? FULL_MASK : (lim <= 0 ? 0u : ((1u << lim) - 1u));
+  }
+  return CH >= 32 ? m : (m & ((1u << CH) - 1u));
+}
+
+// ---------------------------------------------------------------- FP32 filter
+template <int CH>
+__global__ void __launch_bounds__(JOIN_THREADS)
+k_join_f32(const JoinParams P) {
+  extern __shared__ float4 smem_f4[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t nq4 = P.dpad >> 2;
+  float4* sA = smem_f4 + (size_t)w * CH * nq4;
+  const float4* X = (const float4*)P.xs;
+  uint32_t band_cnt = 0, amb_cnt = 0;
+  for (;;) {
+    unsigned long long u = 0;
+    if (lane == 0) u = atomicAdd(&P.ctr->next_unit, 1ull);
+    u = __shfl_sync(FULL_MASK, u, 0);
+    if (u >= P.n_units) break;
+    const Unit U = P.units[u];
+    const uint32_t hs = P.bstart[U.h], he = P.bstart[U.h + 1];
+    const uint32_t a0 = hs + U.chunk * CH;
+    const uint32_t na = min((uint32_t)CH, he - a0);
+    __syncwarp();
+    for (uint32_t i = lane; i < CH * nq4; i += 32)
+      sA[i] = i < na * nq4 ? X[(size_t)a0 * nq4 + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
+    for (uint32_t s = U.s0; s < U.s1; ++s) {
+      const uint32_t b = P.nbr[s];
+      const uint32_t q0 = P.bstart[b], q1 = P.bstart[b + 1];
+      const bool self = (b == U.h);
+      for (uint32_t qb = q0; qb < q1; qb += 32) {
+        const uint32_t q = qb + lane;
+        const bool qv = q < q1;
+        const float4* qrow = X + (size_t)(qv ? q : q0) * nq4;
+        float acc[CH];
+#pragma unroll
+        for (int a = 0; a < CH; ++a) acc[a] = 0.f;
+        for (uint32_t c = 0; c < nq4; ++c) {
+          const float4 qq = qrow[c];
+#pragma unroll
+          for (int a = 0; a < CH; ++a) {
+            const float4 aa = sA[a * nq4 + c];
+            float t;
+            t = aa.x - qq.x; acc[a] = fmaf(t, t, acc[a]);
+            t = aa.y - qq.y; acc[a] = fmaf(t, t, acc[a]);
+            t = aa.z - qq.z; acc[a] = fmaf(t, t, acc[a]);
+            t = aa.w - qq.w; acc[a] = fmaf(t, t, acc[a]);
+          }
+        }
+        uint32_t m = 0;
+#pragma unroll
+        for (int a = 0; a < CH; ++a) m |= (acc[a] <= P.t_hi ? 1u : 0u) << a;
+        m = qv ? (m & home_mask(na, self, q, a0, CH)) : 0u;
+        if (__any_sync(FULL_MASK, m != 0)) {
+          uint32_t lo_m = 0;
+#pragma unroll
+          for (int a = 0; a < CH; ++a) lo_m |= (acc[a] <= P.t_lo ? 1u : 0u) << a;
+          lo_m &= m;
+          uint32_t band = m & ~lo_m, acc_m = lo_m;
+          if (band) {
+            const uint32_t iq = P.ids[q];
+            while (band) {
+              const int a = __ffs(band) - 1;
+              band &= band - 1;
+              const double sd = exact_sqdist(P, P.ids[a0 + a], iq);
+              ++band_cnt;
+              if (fabs(sd - P.eps2) <= P.amb) ++amb_cnt;
+              if (sd <= P.eps2) acc_m |= 1u << a;
+            }
+          }
+          emit_pairs(P, acc_m, a0, q);
+        }
+      }
+    }
+  }
+  add_counter(&P.ctr->band, band_cnt);
+  add_counter(&P.ctr->ambiguous, amb_cnt);
+}
+
+// ---------------------------------------------------------------- FP64 plain
+template <int CH>
+__global__ void __launch_bounds__(JOIN_THREADS)
+k_join_f64(const JoinParams P) {
+  extern __shared__ double2 smem_d2[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t nq2 = P.dpad >> 1;
+  double2* sA = smem_d2 + (size_t)w * CH * nq2;
+  const double2* X = (const double2*)P.xs;
+  const double thr = P.eps2 + P.amb;
+  uint32_t amb_cnt = 0;
+  for (;;) {
+    unsigned long long u = 0;
+    if (lane == 0) u = atomicAdd(&P.ctr->next_unit, 1ull);
+    u = __shfl_sync(FULL_MASK, u, 0);
+    if (u >= P.n_units) break;
+    const Unit U = P.units[u];
+    const uint32_t hs = P.bstart[U.h], he = P.bstart[U.h + 1];
+    const uint32_t a0 = hs + U.chunk * CH;
+    const uint32_t na = min((uint32_t)CH, he - a0);
+    __syncwarp();
+    for (uint32_t i = lane; i < CH * nq2; i += 32)
+      sA[i] = i < na * nq2 ? X[(size_t)a0 * nq2 + i] : make_double2(0.0, 0.0);
+    __syncwarp();
+    for (uint32_t s = U.s0; s < U.s1; ++s) {
+      const uint32_t b = P.nbr[s];
+      const uint32_t q0 = P.bstart[b], q1 = P.bstart[b + 1];
+      const bool self = (b == U.h);
+      for (uint32_t qb = q0; qb < q1; qb += 32) {
+        const uint32_t q = qb + lane;
+        const bool qv = q < q1;
+        const double2* qrow = X + (size_t)(qv ? q : q0) * nq2;
+        double acc[CH];
+#pragma unroll
+        for (int a = 0; a < CH; ++a) acc[a] = 0.0;
+        for (uint32_t c = 0; c < nq2; ++c) {
+          const double2 qq = qrow[c];
+#pragma unroll
+          for (int a = 0; a < CH; ++a) {
+            const double2 aa = sA[a * nq2 + c];
+            double t;
+            t = __dsub_rn(aa.x, qq.x); acc[a] = __dadd_rn(acc[a], __dmul_rn(t, t));
+            t = __dsub_rn(aa.y, qq.y); acc[a] = __dadd_rn(acc[a], __dmul_rn(t, t));
+          }
+        }
+        uint32_t m = 0;
+#pragma unroll
+        for (int a = 0; a < CH; ++a) m |= (acc[a] <= thr ? 1u : 0u) << a;
+        m = qv ? (m & home_mask(na, self, q, a0, CH)) : 0u;
+        if (__any_sync(FULL_MASK, m != 0)) {
+          uint32_t acc_m = 0, amb_m = 0;
+#pragma unroll
+          for (int a = 0; a < CH; ++a) {
+            acc_m |= (acc[a] <= P.eps2 ? 1u : 0u) << a;
+            amb_m |= (fabs(acc[a] - P.eps2) <= P.amb ? 1u : 0u) << a;
+          }
+          acc_m &= m;
+          amb_cnt += __popc(amb_m & m);
+          emit_pairs(P, acc_m, a0, q);
+        }
+      }
+    }
+  }
+  add_counter(&P.ctr->ambiguous, amb_cnt);
+}
+
+// ---------------------------------------------------------------- launcher
+namespace join {
+
+// Home points per unit for a mode and padded width: 32 (FP32) / 16 (FP64)
+// while a warp's staged chunk stays within 16 KB, else 8 / 4.
+int chunk_for(bool fp64, uint32_t dpad) {
+  if (!fp64) return (size_t)32 * dpad * sizeof(float) <= 16 * 1024 ? 32 : 8;
+  return (size_t)16 * dpad * sizeof(double) <= 16 * 1024 ? 16 : 4;
+}
+
+// Persistent launch: warps per block from the shared-memory budget (at most
+// 8, at least 1), blocks = resident blocks per SM x SMs, capped by the work.
+template <class K>
+static void launch_persistent(mistic_handle_s* h, K kern, size_t smem_per_warp, const JoinParams& P,
+                              const char* name) {
+  constexpr size_t kBlockSmem = 200 * 1024;
+  int warps = (int)std::min<size_t>(JOIN_THREADS / 32, std::max<size_t>(1, kBlockSmem / smem_per_warp));
+  const size_t smem = smem_per_warp * warps;
+  if (smem > kBlockSmem + 27 * 1024)
+    throw Error(MISTIC_ERR_TOO_LARGE, "join tile does not fit in shared memory for this dimensionality");
+  if (smem > 48 * 1024) MCK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));
+  if (per_sm < 1) throw Error(MISTIC_ERR_TOO_LARGE, "join kernel does not fit on an SM for this dimensionality");
+  const unsigned long long want = (P.n_units + warps - 1) / warps;
+  const unsigned grid =
+      (unsigned)std::min<unsigned long long>((unsigned long long)per_sm * h->sms, want ? want : 1);
+  kern<<<grid, warps * 32, smem, h->stream>>>(P);
+  launched(h, name);
+}
+
+void run(mistic_handle_s* h, bool fp64, int CH, const JoinParams& P) {
+  if (P.n_units == 0) return;
+  if (!fp64) {
+    const size_t spw = (size_t)CH * P.dpad * sizeof(float);
+    if (CH == 32)
+      launch_persistent(h, k_join_f32<32>, spw, P, "join_f32");
+    else
+      launch_persistent(h, k_join_f32<8>, spw, P, "join_f32");
+  } else {
+    const size_t spw = (size_t)CH * P.dpad * sizeof(double);
+    if (CH == 16)
+      launch_persistent(h, k_join_f64<16>, spw, P, "join_f64");
+    else
+      launch_persistent(h, k_join_f64<4>, spw, P, "join_f64");
+  }
+}
+
+}  // namespace join
+}  // namespace mistic

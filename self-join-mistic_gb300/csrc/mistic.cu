@@ -1,0 +1,668 @@
+// C ABI and pipeline orchestration of the ε-self-join (include/mistic.h).
+//
+// Reference counterpart: nodeLauncher5, src/launcher.cu:3093-3532, which
+// builds the node net on the host (buildNodeNet, src/nodes.cu:5-356),
+// flattens it into CSR arrays, plans batches, copies everything to the
+// device, and per batch launches nodeByPoint5, copies the pair count back,
+// sorts the pairs and rebuilds a host neighbour table.  Here every stage runs
+// on the device on one stream of the handle:
+//
+//   colstats -> (sample covariance) -> reference points (host, small)
+//   -> FP64 RP distances -> packed bin keys -> radix sort -> bin starts
+//   -> sorted-order gather -> ±1 neighbour enumeration (count, scan, fill)
+//   -> persistent join with pair compaction -> (pair sort) -> read-back
+//
+// The host synchronises only for a handful of scalars (key layout, bin and
+// work-list sizes, final counts).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace mistic {
+
+void pairs_to_ij(mistic_handle_s* h, unsigned long long* p, size_t n);
+
+// ------------------------------------------------------------------ plumbing
+
+void throw_cuda(cudaError_t e, const char* what, const char* file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof buf, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    throw Error(MISTIC_ERR_OUT_OF_MEMORY, buf);
+  }
+  throw Error(MISTIC_ERR_CUDA, buf);
+}
+
+void launched(mistic_handle_s* h, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw_cuda(e, what, __FILE__, __LINE__);
+  ++h->launches;
+}
+
+void* Arena::get(const std::string& name, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  Buf& b = bufs[name];
+  if (b.bytes < bytes) {
+    if (b.p) {
+      if (stream) MCK(cudaStreamSynchronize(stream));
+      MCK(cudaFree(b.p));
+    }
+    b.p = nullptr;
+    b.bytes = 0;
+    size_t want = bytes + bytes / 8;  // head-room against regrowth
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      e = cudaMalloc(&b.p, bytes);
+      want = bytes;
+    }
+    if (e != cudaSuccess) throw_cuda(e, ("cudaMalloc " + name).c_str(), __FILE__, __LINE__);
+    b.bytes = want;
+  }
+  return b.p;
+}
+
+void Arena::release_all() {
+  for (auto& kv : bufs)
+    if (kv.second.p) cudaFree(kv.second.p);
+  bufs.clear();
+}
+
+namespace {
+
+template <class T>
+T* abuf(mistic_handle_s* h, const char* name, size_t count) {
+  return (T*)h->arena.get(name, count * sizeof(T));
+}
+
+void d2h(mistic_handle_s* h, void* dst, const void* src, size_t bytes) {
+  MCK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+  MCK(cudaStreamSynchronize(h->stream));
+}
+
+void h2d(mistic_handle_s* h, void* dst, const void* src, size_t bytes) {
+  MCK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
+}
+
+struct PhaseClock {
+  mistic_handle_s* h;
+  bool on;
+  int n = 0;
+  void mark() {
+    if (on && n < 16) MCK(cudaEventRecord(h->ev[n++], h->stream));
+  }
+  double ms(int a, int b) {
+    if (!on || b >= n || a >= n) return 0.0;
+    float v = 0;
+    MCK(cudaEventElapsedTime(&v, h->ev[a], h->ev[b]));
+    return v;
+  }
+};
+
+int bit_length(uint64_t v) {
+  int b = 0;
+  while (v) {
+    ++b;
+    v >>= 1;
+  }
+  return b;
+}
+
+// Threshold pair for the FP32 filter.  With x~ = fl32(x - c), t~ =
+// fl32(x~ - y~), s32 the FP32 fma sum of t~^2, D the exact distance, R the
+// largest ||x~||, u = 2^-24 (inflated for the FP64 centring), the error is
+//   |s32 - D^2| <= E(D) = (1+g_d)(2u(2R+D)D + u^2(2R+D)^2) + g_d D^2 + tiny,
+// g_d = d u / (1 - d u).  The reference value s64 (sequential FP64) obeys
+// |s64 - D^2| <= g64 D^2.  With D' = 1.01 sqrt(eps2), every pair with
+// s32 <= T_lo = eps2/(1+g64) - E(D') has s64 <= eps2, and every pair with
+// s32 > T_hi = eps2/(1-g64) + E(D') has s64 > eps2 (E grows slower than D^2,
+// so pairs with D > D' are beyond T_hi as well); pairs between are re-decided.
+void filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_hi) {
+  const double u = ldexp(1.0, -24) * (1.0 + ldexp(1.0, -20));
+  const double gd = d * u / (1.0 - d * u);
+  const double g64 = (d + 2) * ldexp(1.0, -53) * 1.01;
+  const double Dp = 1.01 * sqrt(eps2);
+  const double tiny = (double)(d + 2) * ldexp(1.0, -126);
+  const double E = (1.0 + gd) * (2.0 * u * (2.0 * R + Dp) * Dp + u * u * (2.0 * R + Dp) * (2.0 * R + Dp)) +
+                   gd * Dp * Dp + tiny;
+  double lo = eps2 / (1.0 + g64) - E;
+  double hi = eps2 / (1.0 - g64) + E;
+  lo *= 1.0 - 1e-12;
+  hi *= 1.0 + 1e-12;
+  float flo = lo > 0 ? (float)lo : -1.0f;
+  if ((double)flo > lo) flo = nextafterf(flo, -INFINITY);
+  float fhi = (float)hi;
+  if ((double)fhi < hi) fhi = nextafterf(fhi, INFINITY);
+  *t_lo = flo;
+  *t_hi = fhi;
+}
+
+void check_handle(mistic_handle h) {
+  if (!h) throw Error(MISTIC_ERR_INVALID_ARG, "null handle");
+  MCK(cudaSetDevice(h->device));
+}
+
+// ------------------------------------------------------------------ the pipeline
+
+void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mistic_dtype dt, uint32_t k,
+                  double eps, const mistic_opts* opts_in, mistic_result* r) {
+  const auto wall0 = std::chrono::steady_clock::now();
+  mistic_opts o;
+  mistic_opts_init(&o);
+  if (opts_in) {
+    if (opts_in->struct_size != sizeof(mistic_opts))
+      throw Error(MISTIC_ERR_INVALID_ARG, "mistic_opts.struct_size mismatch (call mistic_opts_init)");
+    o = *opts_in;
+  }
+  if (!r) throw Error(MISTIC_ERR_INVALID_ARG, "null result");
+  memset(r, 0, sizeof(*r));
+  check_handle(h);
+  if (dt != MISTIC_F64 && dt != MISTIC_F32) throw Error(MISTIC_ERR_INVALID_ARG, "unknown dtype");
+  if (d == 0) throw Error(MISTIC_ERR_INVALID_ARG, "d must be >= 1");
+  if (d > MAX_D) throw Error(MISTIC_ERR_TOO_LARGE, "d above the supported maximum (4096)");
+  if (!(eps >= 0.0) || !std::isfinite(eps)) throw Error(MISTIC_ERR_INVALID_ARG, "eps must be finite and >= 0");
+  if (k > MAX_K) throw Error(MISTIC_ERR_INVALID_ARG, "k above the supported maximum (16)");
+  if (n >= 0xffffffffull) throw Error(MISTIC_ERR_TOO_LARGE, "n must be below 2^32 - 1");
+  if (n > 0 && !pts) throw Error(MISTIC_ERR_INVALID_ARG, "null points");
+  if (o.mode != MISTIC_MODE_AUTO && o.mode != MISTIC_MODE_FP64 && o.mode != MISTIC_MODE_FP32)
+    throw Error(MISTIC_ERR_INVALID_ARG, "unknown mode");
+  if (o.pairs != MISTIC_PAIRS_NONE && o.pairs != MISTIC_PAIRS_HOST && o.pairs != MISTIC_PAIRS_DEVICE)
+    throw Error(MISTIC_ERR_INVALID_ARG, "unknown pairs destination");
+  if (o.input_on_device && n > 0) {
+    cudaPointerAttributes pa;
+    MCK(cudaPointerGetAttributes(&pa, pts));
+    if (pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeManaged)
+      throw Error(MISTIC_ERR_INVALID_ARG, "input_on_device set but pts is not device memory");
+  }
+  const uint32_t launches0 = h->launches;
+  r->n = n;
+  r->d = d;
+  r->mode_used = o.mode;
+  if (n <= 1) {
+    r->pairs_ordered_incl_self = n;
+    r->ms_wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
+    return;
+  }
+  const size_t esz = dt == MISTIC_F64 ? 8 : 4;
+  PhaseClock clk{h, o.timing != 0};
+  clk.mark();  // 0
+
+  // ---- input on the device
+  const void* x = pts;
+  if (!o.input_on_device) {
+    void* dx = h->arena.get("raw", n * d * esz);
+    h2d(h, dx, pts, n * d * esz);
+    x = dx;
+  }
+  clk.mark();  // 1
+
+  // ---- column statistics (+ finiteness) and, for PCA points, a sample covariance
+  const uint32_t cs_parts = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(1, n / 2048), 1024);
+  double* cs_part = abuf<double>(h, "cs_part", (size_t)cs_parts * 3 * d);
+  double* cs_out = abuf<double>(h, "cs_out", 3 * (size_t)d);
+  unsigned* flag = abuf<unsigned>(h, "flag", 4);
+  MCK(cudaMemsetAsync(flag, 0, 4 * sizeof(unsigned), h->stream));
+  idx::colstats(h, x, dt, n, d, cs_part, cs_parts, cs_out, flag);
+  const bool pca = (o.rp_mode == MISTIC_RP_PCA) && k > 0 && d >= 2 && d <= 1024;
+  const uint32_t S = (uint32_t)std::min<uint64_t>(n, d <= 64 ? 8192 : 4096);
+  double* cov = nullptr;
+  if (pca) {
+    double* sbuf = abuf<double>(h, "sample", (size_t)S * d);
+    cov = abuf<double>(h, "cov", (size_t)d * d);
+    idx::sample_cov(h, x, dt, n, d, S, sbuf, cov);
+  }
+  std::vector<double> stats(3 * (size_t)d);
+  unsigned nonfinite = 0;
+  d2h(h, stats.data(), cs_out, stats.size() * sizeof(double));
+  d2h(h, &nonfinite, flag, sizeof(unsigned));
+  if (nonfinite && o.check_finite) throw Error(MISTIC_ERR_NOT_FINITE, "input holds NaN or infinite coordinates");
+  std::vector<double> mean(stats.begin(), stats.begin() + d), mn(stats.begin() + d, stats.begin() + 2 * d),
+      mx(stats.begin() + 2 * d, stats.end());
+  std::vector<double> covh;
+  if (pca) {
+    covh.resize((size_t)d * d);
+    d2h(h, covh.data(), cov, covh.size() * sizeof(double));
+  }
+  std::vector<double> rps;
+  select_reference_points(o, d, k, mean, mn, mx, covh, rps);
+  clk.mark();  // 2
+
+  // ---- FP64 reference-point distances, key layout, packed keys
+  const uint32_t kk = k;
+  double* Dk = nullptr;
+  PackParams pp{};
+  EnumParams ep{};
+  int total_bits = 0, k_used = 0;
+  const double eps2 = eps * eps;
+  if (kk > 0) {
+    double* drp = abuf<double>(h, "rps", (size_t)kk * d);
+    h2d(h, drp, rps.data(), rps.size() * sizeof(double));
+    Dk = abuf<double>(h, "rpdist", n * kk);
+    const uint32_t nparts = (uint32_t)((n + 255) / 256);
+    double* part = abuf<double>(h, "rp_part", (size_t)nparts * 2 * kk);
+    double* mm = abuf<double>(h, "rp_mm", 2 * (size_t)kk);
+    idx::rp_dist(h, x, dt, n, d, drp, (int)kk, Dk, part, nparts, mm);
+    std::vector<double> mmh(2 * (size_t)kk);
+    d2h(h, mmh.data(), mm, mmh.size() * sizeof(double));
+    // Field widths.  δ covers the FP64 error of the distances (relative
+    // (d/2+2)u each), of the difference D - Dmin, and of the quotient.
+    int fields = 0;
+    int bits_acc = 0;
+    int fb[MAX_K];
+    for (uint32_t j = 0; j < kk; ++j) {
+      const double dmin = mmh[j], dmax = mmh[kk + j];
+      const double u64 = ldexp(1.0, -53);
+      const double ratio = eps > 0 ? dmax / eps : 0.0;
+      const double delta = std::max(ldexp(1.0, -20), 8.0 * (d + 4) * u64 * (1.0 + ratio));
+      double w = eps * (1.0 + delta);
+      const double span = dmax - dmin;
+      if (!(w > 0) || span / w > ldexp(1.0, 30)) w = std::max(w, span / ldexp(1.0, 30));
+      if (!(w > 0)) w = 1.0;  // all distances equal: a single field value
+      const double mk = std::min(floor(span / w), ldexp(1.0, 30));
+      if (mk < 1.0) continue;  // uninformative field: every point in the same slot
+      const uint32_t maxkey = (uint32_t)mk;
+      const int b = bit_length(maxkey);
+      if (bits_acc + b > KEY_BITS_MAX) break;
+      pp.col[fields] = (int)j;
+      pp.dmin[fields] = dmin;
+      pp.w[fields] = w;
+      pp.maxkey[fields] = maxkey;
+      ep.maxkey[fields] = maxkey;
+      fb[fields] = b;
+      bits_acc += b;
+      ++fields;
+    }
+    k_used = fields;
+    total_bits = bits_acc;
+    // field 0 is the most significant
+    int sh = total_bits;
+    for (int f = 0; f < fields; ++f) {
+      sh -= fb[f];
+      pp.shift[f] = sh;
+      ep.shift[f] = sh;
+    }
+    pp.k = fields;
+    pp.kstride = (int)kk;
+    ep.k = fields;
+  }
+  r->k_used = (uint32_t)k_used;
+  uint64_t* keys[2] = {abuf<uint64_t>(h, "keys0", n), abuf<uint64_t>(h, "keys1", n)};
+  uint32_t* vals[2] = {abuf<uint32_t>(h, "vals0", n), abuf<uint32_t>(h, "vals1", n)};
+  if (k_used > 0) {
+    idx::pack_keys(h, Dk, n, pp, keys[0]);
+  } else {
+    MCK(cudaMemsetAsync(keys[0], 0, n * sizeof(uint64_t), h->stream));
+  }
+  clk.mark();  // 3
+
+  // ---- sort points by key
+  int cur = 0;
+  if (total_bits > 0) {
+    cur = radix_sort_u64(h, keys, vals, true, true, n, total_bits);
+  } else {
+    idx::iota(h, vals[0], n);
+  }
+  const uint64_t* skeys = keys[cur];
+  const uint32_t* perm = vals[cur];
+  clk.mark();  // 4
+
+  // ---- bins
+  uint32_t* flags = abuf<uint32_t>(h, "binflags", n);
+  uint32_t* nb_dev = abuf<uint32_t>(h, "nbins", 1);
+  uint32_t* bstart = abuf<uint32_t>(h, "bstart", n + 1);
+  uint64_t* bkey = abuf<uint64_t>(h, "bkey", n);
+  idx::bins(h, skeys, n, flags, nb_dev, bstart, bkey);
+  uint32_t m = 0;
+  d2h(h, &m, nb_dev, sizeof(uint32_t));
+  r->n_bins = m;
+
+  // ---- mode and sorted-order gather
+  bool fp64 = (o.mode == MISTIC_MODE_FP64);
+  const uint32_t dpad32 = (d + 3) & ~3u, dpad64 = (d + 1) & ~1u;
+  std::vector<double> center(d, 0.0);
+  if (!fp64)
+    for (uint32_t i = 0; i < d; ++i) center[i] = 0.5 * (mn[i] + mx[i]);
+  double* dcenter = abuf<double>(h, "center", d);
+  h2d(h, dcenter, center.data(), d * sizeof(double));
+  uint32_t* ids = abuf<uint32_t>(h, "ids", n);
+  float* xf = fp64 ? nullptr : abuf<float>(h, "xf", n * dpad32);
+  double* xd = fp64 ? abuf<double>(h, "xd", n * dpad64) : nullptr;
+  const uint32_t gparts = (uint32_t)((n + 255) / 256);
+  double* npart = abuf<double>(h, "norm_part", gparts);
+  double* rmax = abuf<double>(h, "rmax", 1);
+  idx::gather(h, x, dt, n, d, perm, dcenter, fp64 ? 0 : dpad32, xf, fp64 ? dpad64 : 0, xd, ids, npart, rmax);
+  double R2 = 0;
+  d2h(h, &R2, rmax, sizeof(double));
+  const double R = sqrt(R2) * (1.0 + 1e-12);
+  float t_lo = 0, t_hi = 0;
+  if (!fp64) {
+    // FP32 range guard: fall back to the FP64 join when FP32 cannot hold the
+    // coordinates or ε² comfortably.
+    if (R > 1e15 || (eps2 > 0 && eps2 < 1e-28) || eps2 == 0.0) {
+      fp64 = true;
+      xd = abuf<double>(h, "xd", n * dpad64);
+      idx::gather(h, x, dt, n, d, perm, dcenter, 0, nullptr, dpad64, xd, ids, npart, rmax);
+    } else {
+      filter_thresholds(d, eps2, R, &t_lo, &t_hi);
+    }
+  }
+  r->mode_used = fp64 ? MISTIC_MODE_FP64 : MISTIC_MODE_FP32;
+  clk.mark();  // 5
+
+  // ---- neighbour enumeration -> work units
+  const int CH = join::chunk_for(fp64, fp64 ? dpad64 : dpad32);
+  ep.chunk = (uint32_t)CH;
+  ep.seg_cap = 4096;
+  uint32_t* nbr_cnt = abuf<uint32_t>(h, "nbr_cnt", m + 1);
+  uint32_t* unit_cnt = abuf<uint32_t>(h, "unit_cnt", m + 1);
+  unsigned long long* cand = abuf<unsigned long long>(h, "cand", m + 1);
+  idx::enumerate(h, bkey, bstart, m, ep, nbr_cnt, unit_cnt, cand, nullptr, nullptr, nullptr, nullptr, false);
+  uint32_t* tot32 = abuf<uint32_t>(h, "tot32", 2);
+  unsigned long long* tot64 = abuf<unsigned long long>(h, "tot64", 1);
+  exclusive_scan<uint32_t>(h, nbr_cnt, nbr_cnt, m, tot32);
+  exclusive_scan<uint32_t>(h, unit_cnt, unit_cnt, m, tot32 + 1);
+  exclusive_scan<unsigned long long>(h, cand, cand, m, tot64);
+  uint32_t tots[2];
+  unsigned long long totc = 0;
+  d2h(h, tots, tot32, sizeof tots);
+  d2h(h, &totc, tot64, sizeof totc);
+  r->n_bin_pairs = tots[0];
+  r->n_units = tots[1];
+  r->candidates = totc;
+  uint32_t* nbr = abuf<uint32_t>(h, "nbr", (size_t)tots[0] + 1);
+  Unit* units = abuf<Unit>(h, "units", (size_t)tots[1] + 1);
+  idx::enumerate(h, bkey, bstart, m, ep, nullptr, nullptr, nullptr, nbr_cnt, unit_cnt, nbr, units, true);
+  clk.mark();  // 6
+
+  // ---- join
+  JoinParams jp{};
+  jp.units = units;
+  jp.n_units = tots[1];
+  jp.bstart = bstart;
+  jp.nbr = nbr;
+  jp.ids = ids;
+  jp.xs = fp64 ? (const void*)xd : (const void*)xf;
+  jp.dpad = fp64 ? dpad64 : dpad32;
+  jp.raw = x;
+  jp.raw_f32 = dt == MISTIC_F32;
+  jp.d = d;
+  jp.t_lo = t_lo;
+  jp.t_hi = t_hi;
+  jp.eps2 = eps2;
+  jp.amb = 4.0 * (nextafter(eps2, INFINITY) - eps2);
+  JoinCounters* ctr = abuf<JoinCounters>(h, "ctr", 1);
+  const bool want_pairs = o.pairs != MISTIC_PAIRS_NONE;
+  unsigned long long cap = 0;
+  unsigned long long* pbuf = nullptr;
+  const bool caller_buf = want_pairs && o.pairs == MISTIC_PAIRS_DEVICE && o.pair_buffer;
+  if (caller_buf) {
+    if (!o.pair_capacity) throw Error(MISTIC_ERR_INVALID_ARG, "pair_buffer needs pair_capacity > 0");
+    if ((uintptr_t)o.pair_buffer % 8) throw Error(MISTIC_ERR_INVALID_ARG, "pair_buffer must be 8-byte aligned");
+    cap = o.pair_capacity;
+    pbuf = (unsigned long long*)o.pair_buffer;
+  } else if (want_pairs) {
+    cap = o.pair_capacity ? o.pair_capacity : std::max<unsigned long long>(1ull << 20, 16ull * n);
+    auto it = h->arena.bufs.find("pairs");
+    if (!o.pair_capacity && it != h->arena.bufs.end()) cap = std::max<unsigned long long>(cap, it->second.bytes / 8);
+    pbuf = abuf<unsigned long long>(h, "pairs", cap);
+  }
+  jp.pairs = pbuf;
+  jp.cap = cap;
+  jp.ctr = ctr;
+  JoinCounters hc{};
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    MCK(cudaMemsetAsync(ctr, 0, sizeof(JoinCounters), h->stream));
+    join::run(h, fp64, CH, jp);
+    d2h(h, &hc, ctr, sizeof hc);
+    if (!want_pairs || hc.pairs <= cap || o.pair_capacity) break;
+    cap = hc.pairs;
+    pbuf = abuf<unsigned long long>(h, "pairs", cap);
+    jp.pairs = pbuf;
+    jp.cap = cap;
+  }
+  clk.mark();  // 7
+  r->pairs_ij = hc.pairs;
+  r->pairs_ordered_incl_self = 2 * hc.pairs + n;
+  r->band_pairs = fp64 ? 0 : hc.band;
+  r->ulp_ambiguous = hc.ambiguous;
+
+  // ---- pair list
+  mistic_status tail = MISTIC_OK;
+  if (want_pairs) {
+    const unsigned long long stored = std::min<unsigned long long>(hc.pairs, cap);
+    if (hc.pairs > cap) tail = MISTIC_ERR_PAIR_OVERFLOW;
+    if (o.sort_pairs && stored > 1) {
+      uint64_t* pk[2] = {(uint64_t*)pbuf, abuf<uint64_t>(h, "pairs_tmp", stored)};
+      uint32_t* pv[2] = {nullptr, nullptr};
+      const int bits = bit_length(n - 1);
+      int c = radix_sort_u64(h, pk, pv, false, false, stored, 32 + bits);
+      if (c == 1) MCK(cudaMemcpyAsync(pbuf, pk[1], stored * 8, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    pairs_to_ij(h, pbuf, stored);
+    r->pairs_len = stored;
+    if (o.pairs == MISTIC_PAIRS_HOST) {
+      uint32_t* hp = (uint32_t*)malloc(std::max<size_t>(1, stored * 8));
+      if (!hp) throw Error(MISTIC_ERR_OUT_OF_MEMORY, "host pair buffer");
+      MCK(cudaMemcpyAsync(hp, pbuf, stored * 8, cudaMemcpyDeviceToHost, h->stream));
+      MCK(cudaStreamSynchronize(h->stream));
+      r->pairs = hp;
+      r->pairs_on_device = 0;
+      r->_owner = (void*)hp;
+    } else if (caller_buf) {
+      r->pairs = o.pair_buffer;  // caller keeps ownership
+      r->pairs_on_device = 1;
+      r->_owner = nullptr;
+    } else {
+      // hand the device buffer to the result; the arena forgets it
+      h->arena.bufs.erase("pairs");
+      r->pairs = (uint32_t*)pbuf;
+      r->pairs_on_device = 1;
+      r->_owner = (void*)pbuf;
+    }
+  }
+  clk.mark();  // 8
+  MCK(cudaStreamSynchronize(h->stream));
+  r->ms_h2d = clk.ms(0, 1);
+  r->ms_prep = clk.ms(1, 2);
+  r->ms_keys = clk.ms(2, 3);
+  r->ms_sort = clk.ms(3, 4);
+  r->ms_bins = clk.ms(4, 5);
+  r->ms_enum = clk.ms(5, 6);
+  r->ms_join = clk.ms(6, 7);
+  r->ms_d2h = clk.ms(7, 8);
+  r->ms_total = clk.ms(0, 8);
+  r->kernel_launches = h->launches - launches0;
+  r->ms_wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
+  if (tail != MISTIC_OK) throw Error(tail, "pair buffer smaller than the pair count; counts are valid");
+}
+
+}  // namespace
+
+__global__ void k_pairs_to_ij(unsigned long long* p, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long v = p[i];
+  // packed (i << 32 | j) -> memory order (i, j) as two uint32
+  p[i] = (v >> 32) | (v << 32);
+}
+
+void pairs_to_ij(mistic_handle_s* h, unsigned long long* p, size_t n) {
+  if (!n) return;
+  k_pairs_to_ij<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(p, n);
+  launched(h, "pairs_to_ij");
+}
+
+}  // namespace mistic
+
+// ====================================================================== C ABI
+using mistic::Error;
+
+static mistic_status fail(mistic_handle h, mistic_status s, const char* msg) {
+  if (h) h->last_error = msg;
+  return s;
+}
+
+#define MISTIC_GUARD(h, body)                                                   \
+  try {                                                                         \
+    body;                                                                       \
+    return MISTIC_OK;                                                           \
+  } catch (const Error& e) {                                                    \
+    return fail(h, e.status, e.what());                                         \
+  } catch (const std::bad_alloc&) {                                             \
+    return fail(h, MISTIC_ERR_OUT_OF_MEMORY, "host allocation failed");         \
+  } catch (const std::exception& e) {                                           \
+    return fail(h, MISTIC_ERR_INTERNAL, e.what());                              \
+  } catch (...) {                                                               \
+    return fail(h, MISTIC_ERR_INTERNAL, "unknown failure");                     \
+  }
+
+extern "C" {
+
+int mistic_abi_version(void) { return MISTIC_ABI_VERSION; }
+
+void mistic_opts_init(mistic_opts* o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->struct_size = sizeof(mistic_opts);
+  o->mode = MISTIC_MODE_AUTO;
+  o->rp_mode = MISTIC_RP_PCA;
+  o->seed = 0;
+  o->pairs = MISTIC_PAIRS_NONE;
+  o->check_finite = 1;
+  o->timing = 1;
+}
+
+mistic_status mistic_create(mistic_handle* out, int device, void* stream) {
+  if (!out) return MISTIC_ERR_INVALID_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return MISTIC_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= ndev) return MISTIC_ERR_INVALID_ARG;
+  mistic_handle h = new (std::nothrow) mistic_handle_s();
+  if (!h) return MISTIC_ERR_OUT_OF_MEMORY;
+  try {
+    MCK(cudaSetDevice(device));
+    cudaDeviceProp p;
+    MCK(cudaGetDeviceProperties(&p, device));
+    if (p.major < 10) throw Error(MISTIC_ERR_NO_DEVICE, "libmistic is built for sm_103a (Blackwell)");
+    h->device = device;
+    h->sms = p.multiProcessorCount;
+    if (stream) {
+      h->stream = (cudaStream_t)stream;
+    } else {
+      MCK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+      h->own_stream = true;
+    }
+    h->arena.stream = h->stream;
+    for (auto& e : h->ev) MCK(cudaEventCreate(&e));
+  } catch (const Error& e) {
+    mistic_status s = e.status;
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return s;
+  }
+  *out = h;
+  return MISTIC_OK;
+}
+
+mistic_status mistic_destroy(mistic_handle h) {
+  if (!h) return MISTIC_ERR_INVALID_ARG;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  h->arena.release_all();
+  if (h->pinned) cudaFreeHost(h->pinned);
+  for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  if (h->own_stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return MISTIC_OK;
+}
+
+mistic_status mistic_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mistic_dtype dtype,
+                              uint32_t k, double eps, const mistic_opts* opts, mistic_result* result) {
+  MISTIC_GUARD(h, mistic::run_selfjoin(h, pts, n, d, dtype, k, eps, opts, result));
+}
+
+mistic_status mistic_batch_selfjoin(mistic_handle h, const mistic_instance* inst, uint32_t m,
+                                    const mistic_opts* opts, mistic_result* results) {
+  if (!h || (m > 0 && (!inst || !results))) return fail(h, MISTIC_ERR_INVALID_ARG, "null argument");
+  for (uint32_t i = 0; i < m; ++i) {
+    mistic_status s = mistic_selfjoin(h, inst[i].pts, inst[i].n, inst[i].d, inst[i].dtype, inst[i].k,
+                                      inst[i].eps, opts, &results[i]);
+    if (s != MISTIC_OK) return s;
+  }
+  return MISTIC_OK;
+}
+
+mistic_status mistic_read_points(const char* path, uint32_t d, mistic_dtype dtype, void** out_pts,
+                                 uint64_t* out_n) {
+  if (!path || !out_pts || !out_n || d == 0) return MISTIC_ERR_INVALID_ARG;
+  if (dtype != MISTIC_F64 && dtype != MISTIC_F32) return MISTIC_ERR_INVALID_ARG;
+  *out_pts = nullptr;
+  *out_n = 0;
+  std::ifstream f(path, std::ios::in | std::ios::binary);
+  if (!f) return MISTIC_ERR_IO;
+  f.seekg(0, std::ios::end);
+  const std::streamoff size = f.tellg();
+  if (size < 0) return MISTIC_ERR_IO;
+  f.seekg(0, std::ios::beg);
+  const size_t esz = dtype == MISTIC_F64 ? 8 : 4;
+  const uint64_t n = (uint64_t)size / esz / d;
+  void* buf = malloc(std::max<size_t>(1, (size_t)(n * d * esz)));
+  if (!buf) return MISTIC_ERR_OUT_OF_MEMORY;
+  if (n && !f.read((char*)buf, (std::streamsize)(n * d * esz))) {
+    free(buf);
+    return MISTIC_ERR_IO;
+  }
+  *out_pts = buf;
+  *out_n = n;
+  return MISTIC_OK;
+}
+
+void mistic_free_host(void* p) { free(p); }
+
+void mistic_result_free(mistic_result* r) {
+  if (!r) return;
+  if (r->pairs && r->_owner) {
+    if (r->pairs_on_device)
+      cudaFree(r->pairs);
+    else
+      free(r->pairs);
+  }
+  r->pairs = nullptr;
+  r->_owner = nullptr;
+  r->pairs_len = 0;
+}
+
+const char* mistic_strerror(mistic_status s) {
+  switch (s) {
+    case MISTIC_OK: return "ok";
+    case MISTIC_ERR_INVALID_ARG: return "invalid argument";
+    case MISTIC_ERR_CUDA: return "CUDA runtime error";
+    case MISTIC_ERR_OUT_OF_MEMORY: return "out of memory";
+    case MISTIC_ERR_TOO_LARGE: return "problem too large";
+    case MISTIC_ERR_NOT_FINITE: return "non-finite input coordinate";
+    case MISTIC_ERR_PAIR_OVERFLOW: return "pair buffer too small";
+    case MISTIC_ERR_TIMEOUT: return "device wait timed out";
+    case MISTIC_ERR_NO_DEVICE: return "no suitable CUDA device";
+    case MISTIC_ERR_IO: return "I/O error";
+    case MISTIC_ERR_INTERNAL: return "internal error";
+  }
+  return "unknown status";
+}
+
+const char* mistic_last_error(mistic_handle h) { return h ? h->last_error.c_str() : "null handle"; }
+
+}  // extern "C"

@@ -1,0 +1,271 @@
+"""Seeded synthetic point sets for the ε-self-join workloads, and ε calibration.
+
+The reference measures on real datasets (SUSY 5,000,000x18, MSD 515,345x90,
+TINY 5,000,000x384) that are not shipped with it.  These generators produce
+seeded stand-ins with the same shapes and comparable value distributions:
+
+  uniform18     n=100,000  d=18  FP64  i.i.d. U[0,1)^18, seed 0, k=6, 32 nbrs
+  susy18        n=5,000,000 d=18 FP64  8 lognormal(sigma=0.8) raw columns plus
+                10 seeded nonlinear combinations of them with N(0,0.05) noise,
+                every column min-max scaled to [0,1]; k=6, 64 nbrs
+  msd90         n=515,345  d=90  FP64  correlated Gaussian (random orthogonal
+                basis, spectrum i^-1.2), column-standardised; k=8, 16 nbrs
+  batch2000     2,000 independent instances, n log-uniform in [1e3, 2e5],
+                d in {2,8,18,32,57,90}, FP32 anisotropic Gaussian mixtures
+  tiny384       n=5,000,000 d=384 FP32, 1,000 Zipf(1.1)-sized anisotropic
+                Gaussian clusters, L2-normalised; k=8, 16 nbrs
+
+ε is calibrated by bisection on a seeded 10,000-point sample: the mean
+neighbour count of the full set is estimated as (n-1)/(|S|-1) times the mean
+within-sample FP64 neighbour count (self excluded), and ε is bisected in FP64
+for 60 iterations to the smallest value whose estimate reaches the target.
+The calibrated ε is stored as a hex float so every implementation uses the
+identical value.
+
+The reference reads a raw little-endian FP64 row-major file whose row count
+is bytes/8/d (src/main.cu:42-50); `write_bin`/`read_bin` follow that format.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# ---------------------------------------------------------------- file format
+
+
+def write_bin(path: str, pts: np.ndarray) -> None:
+    """Write points as the reference's input file: raw little-endian FP64,
+    row-major, no header (src/main.cu:42-50)."""
+    np.ascontiguousarray(pts, dtype="<f8").tofile(path)
+
+
+def read_bin(path: str, d: int, dtype: str = "<f8") -> np.ndarray:
+    """Read a raw row-major point file; n = bytes / itemsize / d, any trailing
+    partial row is ignored exactly as the reference's integer division does
+    (src/main.cu:50)."""
+    raw = np.fromfile(path, dtype=dtype)
+    n = raw.size // d
+    return raw[: n * d].reshape(n, d)
+
+
+# ---------------------------------------------------------------- generators
+
+
+def gen_uniform(n: int = 100_000, d: int = 18, seed: int = 0) -> np.ndarray:
+    """i.i.d. U[0,1)^d from numpy PCG64 with the given seed."""
+    return np.random.default_rng(seed).random((n, d))
+
+
+def gen_susy_like(n: int = 5_000_000, d_raw: int = 8, d_derived: int = 10,
+                  seed: int = 2) -> np.ndarray:
+    """Heavy-tailed positive raw features plus nonlinear derived features,
+    each column min-max normalised to [0,1] (SUSY-shaped, d = 18)."""
+    rng = np.random.default_rng(seed)
+    spec_rng = np.random.default_rng(seed + 1000)
+    spec = [tuple(spec_rng.choice(d_raw, size=3, replace=False)) for _ in range(d_derived)]
+    x = np.empty((n, d_raw + d_derived), dtype=np.float64)
+    chunk = 1 << 18
+    for r0 in range(0, n, chunk):  # chunked: bounded temporaries
+        m = min(chunk, n - r0)
+        raw = rng.lognormal(mean=0.0, sigma=0.8, size=(m, d_raw))
+        noise = rng.normal(0.0, 0.05, size=(m, d_derived))
+        out = x[r0:r0 + m]
+        out[:, :d_raw] = raw
+        for t, (a, b, c) in enumerate(spec):
+            kind = t % 3
+            if kind == 0:      # product
+                v = raw[:, a] * raw[:, b]
+            elif kind == 1:    # ratio
+                v = raw[:, a] / (raw[:, b] + 0.5)
+            else:              # sqrt of a sum of squares
+                v = np.sqrt(raw[:, a] ** 2 + raw[:, b] ** 2 + raw[:, c] ** 2)
+            out[:, d_raw + t] = v + noise[:, t]
+    lo = x.min(axis=0)
+    hi = x.max(axis=0)
+    x -= lo
+    x /= (hi - lo)
+    return x
+
+
+def gen_msd_like(n: int = 515_345, d: int = 90, seed: int = 3) -> np.ndarray:
+    """Correlated Gaussian: random orthogonal basis times a spectrum decaying
+    as i^-1.2, then column-standardised (MSD-shaped, d = 90)."""
+    rng = np.random.default_rng(seed)
+    q, _ = np.linalg.qr(rng.normal(size=(d, d)))
+    scale = np.arange(1, d + 1, dtype=np.float64) ** -0.6  # sqrt of i^-1.2
+    z = rng.normal(size=(n, d)) * scale
+    x = z @ q.T
+    x = (x - x.mean(axis=0)) / x.std(axis=0)
+    return x
+
+
+def gen_clusters(n: int, d: int, n_clusters: int, seed: int,
+                 zipf: float | None = None, normalise: bool = False,
+                 eig_lo: float = 1e-3, eig_hi: float = 1.0,
+                 dtype=np.float32) -> np.ndarray:
+    """Gaussian mixture with per-cluster random rotation and log-uniform
+    eigenvalues; cluster sizes Zipf(zipf) when given, else multinomial."""
+    rng = np.random.default_rng(seed)
+    if zipf is not None:
+        w = 1.0 / np.arange(1, n_clusters + 1, dtype=np.float64) ** zipf
+    else:
+        w = rng.random(n_clusters) + 0.1
+    w /= w.sum()
+    sizes = rng.multinomial(n, w)
+    out = np.empty((n, d), dtype=dtype)
+    pos = 0
+    centres = rng.normal(size=(n_clusters, d))
+    for c in range(n_clusters):
+        m = int(sizes[c])
+        if m == 0:
+            continue
+        # random rotation restricted to a low-rank frame keeps this cheap for
+        # d = 384: the covariance is R diag(eig) R^T with R a random
+        # orthogonal basis of a min(d, 32)-dimensional subspace plus isotropic
+        # floor eig_lo on the complement.
+        r = min(d, 32)
+        basis, _ = np.linalg.qr(rng.normal(size=(d, r)))
+        eig = np.exp(rng.uniform(math.log(eig_lo), math.log(eig_hi), size=r))
+        z = rng.normal(size=(m, r)) * np.sqrt(eig)
+        pts = centres[c] * 0.5 + z @ basis.T
+        pts += rng.normal(scale=math.sqrt(eig_lo), size=(m, d))
+        out[pos:pos + m] = pts
+        pos += m
+    perm = rng.permutation(n)
+    out = out[perm]
+    if normalise:
+        nrm = np.linalg.norm(out.astype(np.float64), axis=1, keepdims=True)
+        out = (out / nrm).astype(dtype)
+    return out
+
+
+# ---------------------------------------------------------------- ε calibration
+
+
+def _within_sample_sqdist(s: np.ndarray) -> np.ndarray:
+    """All unordered i<j squared FP64 distances within the sample, sorted."""
+    s = np.ascontiguousarray(s, dtype=np.float64)
+    m = s.shape[0]
+    nrm = np.einsum("ij,ij->i", s, s)
+    out = []
+    blk = 1024
+    for i0 in range(0, m, blk):
+        a = s[i0:i0 + blk]
+        g = a @ s.T
+        d2 = nrm[i0:i0 + blk, None] + nrm[None, :] - 2.0 * g
+        rows = np.arange(i0, min(i0 + blk, m))[:, None]
+        mask = np.arange(m)[None, :] > rows
+        out.append(d2[mask])
+    d2 = np.concatenate(out)
+    np.maximum(d2, 0.0, out=d2)
+    d2.sort()
+    return d2
+
+
+def calibrate_eps(pts: np.ndarray, target_mean: float, sample: int = 10_000,
+                  seed: int = 12345, iters: int = 60) -> float:
+    """Bisect ε in FP64 so that the sample-extrapolated mean neighbour count
+    (self excluded) reaches `target_mean`."""
+    n = pts.shape[0]
+    rng = np.random.default_rng(seed)
+    m = min(sample, n)
+    idx = np.sort(rng.choice(n, size=m, replace=False))
+    d2 = _within_sample_sqdist(pts[idx])
+    scale = (n - 1) / max(m - 1, 1)
+
+    def est(eps: float) -> float:
+        cnt = np.searchsorted(d2, eps * eps, side="right")  # unordered pairs
+        return 2.0 * cnt / m * scale
+
+    lo, hi = 0.0, float(math.sqrt(d2[-1])) * 1.0001 + 1e-300
+    for _ in range(iters):
+        mid = 0.5 * (lo + hi)
+        if est(mid) >= target_mean:
+            hi = mid
+        else:
+            lo = mid
+    return hi
+
+
+# ---------------------------------------------------------------- configs
+
+
+@dataclass
+class Workload:
+    """One self-join instance: points (n x d), reference-point count k, ε."""
+    name: str
+    pts: np.ndarray
+    k: int
+    eps: float
+    target_mean: float
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return int(self.pts.shape[0])
+
+    @property
+    def d(self) -> int:
+        return int(self.pts.shape[1])
+
+
+#: ε values calibrated once with calibrate_eps (stored as hex floats so every
+#: implementation uses the identical value).  Filled lazily when absent.
+EPS_HEX: dict[str, str] = {
+    "uniform18:100000": "0x1.c37b06bdae65ep-1",
+    "susy18:5000000": "0x1.55e138a251ac5p-7",
+}
+
+
+def _eps_for(name: str, pts: np.ndarray, target: float) -> float:
+    if name in EPS_HEX:
+        return float.fromhex(EPS_HEX[name])
+    e = calibrate_eps(pts, target)
+    EPS_HEX[name] = e.hex()
+    return e
+
+
+def uniform18(n: int = 100_000) -> Workload:
+    pts = gen_uniform(n, 18, seed=0)
+    key = f"uniform18:{n}"
+    return Workload(key, pts, 6, _eps_for(key, pts, 32.0), 32.0)
+
+
+def susy18(n: int = 5_000_000) -> Workload:
+    pts = gen_susy_like(n)
+    key = f"susy18:{n}"
+    return Workload(key, pts, 6, _eps_for(key, pts, 64.0), 64.0)
+
+
+def msd90(n: int = 515_345) -> Workload:
+    pts = gen_msd_like(n)
+    key = f"msd90:{n}"
+    return Workload(key, pts, 8, _eps_for(key, pts, 16.0), 16.0)
+
+
+def tiny384(n: int = 5_000_000) -> Workload:
+    pts = gen_clusters(n, 384, 1000, seed=5, zipf=1.1, normalise=True)
+    key = f"tiny384:{n}"
+    return Workload(key, pts, 8, _eps_for(key, pts, 16.0), 16.0)
+
+
+def batch_instances(count: int = 2000, seed: int = 7, n_lo: int = 1_000,
+                    n_hi: int = 200_000) -> list[Workload]:
+    """Uneven independent instances: n log-uniform in [n_lo, n_hi], d in
+    {2,8,18,32,57,90}, FP32 Gaussian mixtures of 1-50 anisotropic clusters,
+    mean neighbour target in {4,16,64}.  Per-instance seeds derive from
+    (seed, index)."""
+    master = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(round(math.exp(master.uniform(math.log(n_lo), math.log(n_hi)))))
+        d = int(master.choice([2, 8, 18, 32, 57, 90]))
+        nc = int(master.integers(1, 51))
+        tgt = float(master.choice([4.0, 16.0, 64.0]))
+        pts = gen_clusters(n, d, nc, seed=seed * 100_003 + i, eig_lo=1e-2)
+        eps = calibrate_eps(pts, tgt, sample=min(n, 4000), seed=i)
+        out.append(Workload(f"batch{i}", pts, min(6, d), eps, tgt,
+                            {"index": i}))
+    return out

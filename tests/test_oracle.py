@@ -1,0 +1,69 @@
+"""The oracle against the reference's own results (CPU only).
+
+golden.json holds, per seeded case, the ordered-with-self pair count the
+reference's brute_force (src/utils.cu:285-317) printed when compiled from its
+unmodified source, plus the oracle's canonical pair-list hash."""
+import numpy as np
+import pytest
+
+from helpers import canon, case_input, input_sha, pairs_sha
+from oracle import oracle as O
+
+
+def test_golden_cases_cover_edges(golden):
+    names = {c["name"] for c in golden}
+    assert any("ties" in n for n in names)
+    assert any(c.get("eps") == 0.0 for c in golden)
+    assert any(c.get("f32") for c in golden)
+    assert any(c["k"] == 0 for c in golden)
+    assert len(golden) >= 12
+
+
+@pytest.mark.parametrize("idx", range(15))
+def test_oracle_matches_reference_counts(golden, idx):
+    c = golden[idx]
+    x = case_input(c)
+    if input_sha(x) != c["input_sha256"]:
+        pytest.skip("generator output differs from the fixture on this numpy")
+    eps = float.fromhex(c["eps_hex"])
+    pairs = O.brute_pairs(x, eps)
+    assert 2 * len(pairs) + c["n"] == c["ref_ordered_incl_self"]
+    assert pairs_sha(pairs) == c["oracle_pairs_sha256"]
+    # canonical order and i < j
+    assert np.array_equal(pairs, canon(pairs))
+    if len(pairs):
+        assert (pairs[:, 0] < pairs[:, 1]).all()
+
+
+def test_ordered_count_is_reference_number(golden):
+    c = golden[0]
+    x = case_input(c)
+    eps = float.fromhex(c["eps_hex"])
+    assert O.count_ordered(x, eps) == c["ref_ordered_incl_self"]
+
+
+def test_query_pairs_subset_of_full():
+    rng = np.random.default_rng(3)
+    x = rng.random((800, 5))
+    eps = 0.2
+    full = O.brute_pairs(x, eps)
+    q = np.array([0, 17, 400, 799], dtype=np.uint32)
+    part = O.query_pairs(x, eps, q)
+    sel = full[np.isin(full[:, 0], q) | np.isin(full[:, 1], q)]
+    assert np.array_equal(canon(part), canon(sel))
+
+
+def test_predicate_is_sequential_rounded_sum():
+    # (a - b)^2 summed left to right with each op rounded: check one pair by hand
+    x = np.array([[0.1, 0.2, 0.3], [0.4, 0.6, 0.9]])
+    s = 0.0
+    for t in range(3):
+        df = x[0, t] - x[1, t]
+        s = s + df * df
+    assert O.sqdist(x, 0, 1) == s
+
+
+def test_empty_and_single():
+    assert len(O.brute_pairs(np.zeros((0, 3)), 1.0)) == 0
+    assert len(O.brute_pairs(np.zeros((1, 3)), 1.0)) == 0
+    assert len(O.brute_pairs(np.zeros((2, 3)), 0.0)) == 1
