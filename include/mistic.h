@@ -180,6 +180,38 @@ void mistic_result_free(mistic_result* r);
 const char* mistic_strerror(mistic_status s);
 const char* mistic_last_error(mistic_handle h);
 
+/* ---- No-allocation entry point.  This one has no counterpart in the
+ * reference; it exists for callers that must not allocate device memory
+ * while they run: a service whose device memory is reserved up front by its
+ * own pool allocator (a fresh cudaMalloc can fail or fragment that pool), or
+ * a latency-critical path where the implicit device-wide synchronisation of
+ * cudaMalloc/cudaFree would stall other streams.
+ *
+ * The same exact ε-self-join (every pair i < j is a candidate: no reference-
+ * point index, O(n^2) work, meant for modest n), with the points already on
+ * the device (d_pts, row-major n x d) and the pair list written into the
+ * caller's device buffer d_pairs (pair_capacity pairs of uint32 (i, j),
+ * i < j, unsorted, 8-byte aligned).  *pairs_ij receives the pair count; the
+ * call returns MISTIC_ERR_PAIR_OVERFLOW when it exceeds pair_capacity (the
+ * count stays valid).  Runs on `stream` (a cudaStream_t, NULL = default
+ * stream) on the current device and returns when the work is done.
+ *
+ * It calls no cudaMalloc/cudaFree and no allocating library routine: its only
+ * scratch is one file-scope device array of MISTIC_NOALLOC_SCRATCH_BYTES
+ * that every GPU which loads the library holds until the process exits.  The
+ * scratch holds an FP32 copy of the points, so n * ceil4(d) * 4 bytes must fit
+ * in it minus 256 bytes (e.g. n <= 419,427 at d = 18), and d must be at most
+ * MISTIC_NOALLOC_MAX_D; larger inputs are rejected with MISTIC_ERR_TOO_LARGE.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current: make it before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU (from
+ * several streams or host threads) race; serialise them. */
+#define MISTIC_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+#define MISTIC_NOALLOC_MAX_D 128u
+mistic_status mistic_selfjoin_noalloc(const void* d_pts, uint64_t n, uint32_t d, mistic_dtype dtype,
+                                      double eps, uint32_t* d_pairs, uint64_t pair_capacity,
+                                      uint64_t* pairs_ij, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -174,6 +174,11 @@ void enumerate(mistic_handle_s*, const uint64_t* bkey, const uint32_t* bstart, u
                bool fill);
 }  // namespace idx
 
+// ---- mistic.cu: FP32 filter thresholds (accept at or below t_lo, re-decide
+// in FP64 above it up to t_hi) for dimension d, eps2 = fl(ε*ε) and largest
+// centred FP32 row norm R.
+void filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_hi);
+
 // ---- join.cu
 namespace join {
 int chunk_for(bool fp64, uint32_t dpad);

@@ -77,6 +77,35 @@ void Arena::release_all() {
   bufs.clear();
 }
 
+// Threshold pair for the FP32 filter.  With x~ = fl32(x - c), t~ =
+// fl32(x~ - y~), s32 the FP32 fma sum of t~^2, D the exact distance, R the
+// largest ||x~||, u = 2^-24 (inflated for the FP64 centring), the error is
+//   |s32 - D^2| <= E(D) = (1+g_d)(2u(2R+D)D + u^2(2R+D)^2) + g_d D^2 + tiny,
+// g_d = d u / (1 - d u).  The reference value s64 (sequential FP64) obeys
+// |s64 - D^2| <= g64 D^2.  With D' = 1.01 sqrt(eps2), every pair with
+// s32 <= T_lo = eps2/(1+g64) - E(D') has s64 <= eps2, and every pair with
+// s32 > T_hi = eps2/(1-g64) + E(D') has s64 > eps2 (E grows slower than D^2,
+// so pairs with D > D' are beyond T_hi as well); pairs between are re-decided.
+void filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_hi) {
+  const double u = ldexp(1.0, -24) * (1.0 + ldexp(1.0, -20));
+  const double gd = d * u / (1.0 - d * u);
+  const double g64 = (d + 2) * ldexp(1.0, -53) * 1.01;
+  const double Dp = 1.01 * sqrt(eps2);
+  const double tiny = (double)(d + 2) * ldexp(1.0, -126);
+  const double E = (1.0 + gd) * (2.0 * u * (2.0 * R + Dp) * Dp + u * u * (2.0 * R + Dp) * (2.0 * R + Dp)) +
+                   gd * Dp * Dp + tiny;
+  double lo = eps2 / (1.0 + g64) - E;
+  double hi = eps2 / (1.0 - g64) + E;
+  lo *= 1.0 - 1e-12;
+  hi *= 1.0 + 1e-12;
+  float flo = lo > 0 ? (float)lo : -1.0f;
+  if ((double)flo > lo) flo = nextafterf(flo, -INFINITY);
+  float fhi = (float)hi;
+  if ((double)fhi < hi) fhi = nextafterf(fhi, INFINITY);
+  *t_lo = flo;
+  *t_hi = fhi;
+}
+
 namespace {
 
 template <class T>
@@ -115,35 +144,6 @@ int bit_length(uint64_t v) {
     v >>= 1;
   }
   return b;
-}
-
-// Threshold pair for the FP32 filter.  With x~ = fl32(x - c), t~ =
-// fl32(x~ - y~), s32 the FP32 fma sum of t~^2, D the exact distance, R the
-// largest ||x~||, u = 2^-24 (inflated for the FP64 centring), the error is
-//   |s32 - D^2| <= E(D) = (1+g_d)(2u(2R+D)D + u^2(2R+D)^2) + g_d D^2 + tiny,
-// g_d = d u / (1 - d u).  The reference value s64 (sequential FP64) obeys
-// |s64 - D^2| <= g64 D^2.  With D' = 1.01 sqrt(eps2), every pair with
-// s32 <= T_lo = eps2/(1+g64) - E(D') has s64 <= eps2, and every pair with
-// s32 > T_hi = eps2/(1-g64) + E(D') has s64 > eps2 (E grows slower than D^2,
-// so pairs with D > D' are beyond T_hi as well); pairs between are re-decided.
-void filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_hi) {
-  const double u = ldexp(1.0, -24) * (1.0 + ldexp(1.0, -20));
-  const double gd = d * u / (1.0 - d * u);
-  const double g64 = (d + 2) * ldexp(1.0, -53) * 1.01;
-  const double Dp = 1.01 * sqrt(eps2);
-  const double tiny = (double)(d + 2) * ldexp(1.0, -126);
-  const double E = (1.0 + gd) * (2.0 * u * (2.0 * R + Dp) * Dp + u * u * (2.0 * R + Dp) * (2.0 * R + Dp)) +
-                   gd * Dp * Dp + tiny;
-  double lo = eps2 / (1.0 + g64) - E;
-  double hi = eps2 / (1.0 - g64) + E;
-  lo *= 1.0 - 1e-12;
-  hi *= 1.0 + 1e-12;
-  float flo = lo > 0 ? (float)lo : -1.0f;
-  if ((double)flo > lo) flo = nextafterf(flo, -INFINITY);
-  float fhi = (float)hi;
-  if ((double)fhi < hi) fhi = nextafterf(fhi, INFINITY);
-  *t_lo = flo;
-  *t_hi = fhi;
 }
 
 void check_handle(mistic_handle h) {

@@ -29,8 +29,12 @@ EXPORTS = (
     "mistic_abi_version", "mistic_opts_init", "mistic_create", "mistic_destroy",
     "mistic_selfjoin", "mistic_batch_selfjoin", "mistic_read_points",
     "mistic_free_host", "mistic_result_free", "mistic_strerror",
-    "mistic_last_error",
+    "mistic_last_error", "mistic_selfjoin_noalloc",
 )
+
+#: scratch limits of mistic_selfjoin_noalloc (include/mistic.h)
+NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
+NOALLOC_MAX_D = 128
 
 
 class Opts(ctypes.Structure):
@@ -124,5 +128,8 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
     L.mistic_strerror.restype = ctypes.c_char_p
     L.mistic_last_error.argtypes = [vp]
     L.mistic_last_error.restype = ctypes.c_char_p
+    L.mistic_selfjoin_noalloc.argtypes = [vp, u64, u32, ctypes.c_int, dbl, vp, u64,
+                                          ctypes.POINTER(u64), vp]
+    L.mistic_selfjoin_noalloc.restype = ctypes.c_int
     _lib = L
     return L
