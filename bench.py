@@ -52,10 +52,25 @@ METRIC = "self-join wall time & distance evals/s: mixed-prec vs FP64 plain, exac
 UNIT = "points/s"
 
 #: workload name -> (constructor, description)
+def _subset(make, full_n):
+    """The workload at full size, or its first n points with the full
+    configuration's ε (a smaller case of the same kernel, for profiling)."""
+    def f(n):
+        if not n or n == full_n:
+            return make(full_n)
+        full_eps = float.fromhex(W.EPS_HEX[f"{make.__name__}:{full_n}"])
+        wl = make.__wrapped_gen__(n)
+        return W.Workload(f"{make.__name__}:{n}", wl[0], wl[1], full_eps, wl[2])
+    return f
+
+
+W.susy18.__wrapped_gen__ = lambda n: (W.gen_susy_like(n), 6, 64.0)
+W.uniform18.__wrapped_gen__ = lambda n: (W.gen_uniform(n, 18, seed=0), 6, 32.0)
+
 WORKLOADS = {
-    "susy18": (lambda n: W.susy18(n or 5_000_000),
+    "susy18": (_subset(W.susy18, 5_000_000),
                "SUSY-shaped n=5e6 d=18 FP64, k=6, 64 mean neighbours"),
-    "uniform18": (lambda n: W.uniform18(n or 100_000),
+    "uniform18": (_subset(W.uniform18, 100_000),
                   "uniform n=1e5 d=18 FP64, k=6, 32 mean neighbours"),
 }
 

@@ -94,8 +94,8 @@ __device__ __forceinline__ void add_counter(unsigned long long* c, uint32_t v) {
   if (lane == 0 && s) atomicAdd(c, (unsigned long long)s);
 }
 
-// Valid-home mask for candidate q: home points a0 .. a0+na-1, and in the
-// home bin itself only pairs with sorted position a < q.
+// Valid-home mask for candidate q: home points a0 .. a0+na-1, and when q
+// lies in the home bin itself only pairs with sorted position a < q.
 __device__ __forceinline__ uint32_t home_mask(uint32_t na, bool self, uint32_t q, uint32_t a0, int CH) {
   uint32_t m = na >= 32 ? FULL_MASK : ((1u << na) - 1u);
   if (self) {
@@ -105,7 +105,104 @@ __device__ __forceinline__ uint32_t home_mask(uint32_t na, bool self, uint32_t q
   return CH >= 32 ? m : (m & ((1u << CH) - 1u));
 }
 
+// Candidate stream of one unit: the points of the neighbour bins
+// nbr[s .. s1) in order, 32 per tile, lanes filled across bin boundaries
+// (bins average a few points, so one bin per tile would leave most lanes
+// idle).  `s` and `off` (next bin, offset inside it) are warp-uniform.
+// Each lane gets its candidate's sorted position q, or qv = false past the
+// end.  Lane l finds its bin by a binary search over the warp's inclusive
+// scan of up to 32 bin sizes.
+struct CandTile {
+  uint32_t q;
+  bool qv;
+};
+
+__device__ __forceinline__ CandTile next_tile(const JoinParams& P, uint32_t& s, uint32_t& off, uint32_t s1) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t bj = s + lane;
+  uint32_t start = 0, size = 0;
+  if (bj < s1) {
+    const uint32_t b = P.nbr[bj];
+    start = P.bstart[b];
+    size = P.bstart[b + 1] - start;
+    if (lane == 0) {
+      start += off;
+      size -= off;
+    }
+  }
+  const uint32_t incl = warp_incl_scan_u32(size);
+  const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+  // j = first window bin whose inclusive end exceeds this lane's rank
+  int lo = 0, hi = 31;
+#pragma unroll
+  for (int it = 0; it < 5; ++it) {
+    const int mid = (lo + hi) >> 1;
+    const uint32_t v = __shfl_sync(FULL_MASK, incl, mid);
+    if (v <= (uint32_t)lane) lo = mid + 1; else hi = mid;
+  }
+  const int j = lo;
+  const uint32_t sj = __shfl_sync(FULL_MASK, start, j);
+  const uint32_t ej = __shfl_sync(FULL_MASK, incl, j);
+  const uint32_t zj = __shfl_sync(FULL_MASK, size, j);
+  CandTile t;
+  t.qv = (uint32_t)lane < total;
+  t.q = sj + (uint32_t)lane - (ej - zj);
+  // advance past the 32 candidates handed out
+  if (total > 32) {
+    const int j31 = __shfl_sync(FULL_MASK, j, 31);
+    const uint32_t e31 = __shfl_sync(FULL_MASK, ej, 31), z31 = __shfl_sync(FULL_MASK, zj, 31);
+    const uint32_t used = 32 - (e31 - z31);  // candidates taken from bin j31
+    if (used < z31) {
+      off = (j31 == 0 ? off : 0u) + used;
+      s += j31;
+    } else {
+      off = 0;
+      s += j31 + 1;
+    }
+  } else {
+    s = min(s + 32, s1);
+    off = 0;
+  }
+  return t;
+}
+
 // ---------------------------------------------------------------- FP32 filter
+// Distance of lane candidate (qrow) to the CH staged home rows, dims
+// [0, d): full float4 chunks, then a 1-3 wide tail; home rows beyond na are
+// skipped (warp-uniform), their accumulators stay unused.
+template <int CH>
+__device__ __forceinline__ void f32_dists(const float4* __restrict__ qrow, const float4* sA, uint32_t nq4,
+                                          uint32_t d, uint32_t na, float (&acc)[CH]) {
+  const uint32_t full = d >> 2, tail = d & 3;
+#pragma unroll
+  for (int a = 0; a < CH; ++a) acc[a] = 0.f;
+  for (uint32_t c = 0; c < full; ++c) {
+    const float4 qq = qrow[c];
+#pragma unroll
+    for (int a = 0; a < CH; ++a) {
+      if (a >= (int)na) break;
+      const float4 aa = sA[a * nq4 + c];
+      float t;
+      t = aa.x - qq.x; acc[a] = fmaf(t, t, acc[a]);
+      t = aa.y - qq.y; acc[a] = fmaf(t, t, acc[a]);
+      t = aa.z - qq.z; acc[a] = fmaf(t, t, acc[a]);
+      t = aa.w - qq.w; acc[a] = fmaf(t, t, acc[a]);
+    }
+  }
+  if (tail) {
+    const float4 qq = qrow[full];
+#pragma unroll
+    for (int a = 0; a < CH; ++a) {
+      if (a >= (int)na) break;
+      const float4 aa = sA[a * nq4 + full];
+      float t;
+      t = aa.x - qq.x; acc[a] = fmaf(t, t, acc[a]);
+      if (tail > 1) { t = aa.y - qq.y; acc[a] = fmaf(t, t, acc[a]); }
+      if (tail > 2) { t = aa.z - qq.z; acc[a] = fmaf(t, t, acc[a]); }
+    }
+  }
+}
+
 template <int CH>
 __global__ void __launch_bounds__(JOIN_THREADS)
 k_join_f32(const JoinParams P) {
@@ -128,52 +225,123 @@ k_join_f32(const JoinParams P) {
     for (uint32_t i = lane; i < CH * nq4; i += 32)
       sA[i] = i < na * nq4 ? X[(size_t)a0 * nq4 + i] : make_float4(0.f, 0.f, 0.f, 0.f);
     __syncwarp();
-    for (uint32_t s = U.s0; s < U.s1; ++s) {
-      const uint32_t b = P.nbr[s];
-      const uint32_t q0 = P.bstart[b], q1 = P.bstart[b + 1];
-      const bool self = (b == U.h);
-      for (uint32_t qb = q0; qb < q1; qb += 32) {
-        const uint32_t q = qb + lane;
-        const bool qv = q < q1;
-        const float4* qrow = X + (size_t)(qv ? q : q0) * nq4;
-        float acc[CH];
+    uint32_t s = U.s0, off = 0;
+    while (s < U.s1) {
+      const CandTile t = next_tile(P, s, off, U.s1);
+      const uint32_t q = t.q;
+      const float4* qrow = X + (size_t)(t.qv ? q : a0) * nq4;
+      float acc[CH];
+      f32_dists<CH>(qrow, sA, nq4, P.d, na, acc);
+      uint32_t m = 0;
 #pragma unroll
-        for (int a = 0; a < CH; ++a) acc[a] = 0.f;
-        for (uint32_t c = 0; c < nq4; ++c) {
-          const float4 qq = qrow[c];
+      for (int a = 0; a < CH; ++a) {
+        if (a >= (int)na) break;
+        m |= (acc[a] <= P.t_hi ? 1u : 0u) << a;
+      }
+      m = t.qv ? (m & home_mask(na, q >= hs && q < he, q, a0, CH)) : 0u;
+      if (__any_sync(FULL_MASK, m != 0)) {
+        uint32_t lo_m = 0;
 #pragma unroll
-          for (int a = 0; a < CH; ++a) {
-            const float4 aa = sA[a * nq4 + c];
-            float t;
-            t = aa.x - qq.x; acc[a] = fmaf(t, t, acc[a]);
-            t = aa.y - qq.y; acc[a] = fmaf(t, t, acc[a]);
-            t = aa.z - qq.z; acc[a] = fmaf(t, t, acc[a]);
-            t = aa.w - qq.w; acc[a] = fmaf(t, t, acc[a]);
+        for (int a = 0; a < CH; ++a) {
+          if (a >= (int)na) break;
+          lo_m |= (acc[a] <= P.t_lo ? 1u : 0u) << a;
+        }
+        lo_m &= m;
+        uint32_t band = m & ~lo_m, acc_m = lo_m;
+        if (band) {
+          const uint32_t iq = P.ids[q];
+          while (band) {
+            const int a = __ffs(band) - 1;
+            band &= band - 1;
+            const double sd = exact_sqdist(P, P.ids[a0 + a], iq);
+            ++band_cnt;
+            if (fabs(sd - P.eps2) <= P.amb) ++amb_cnt;
+            if (sd <= P.eps2) acc_m |= 1u << a;
           }
         }
-        uint32_t m = 0;
+        emit_pairs(P, acc_m, a0, q);
+      }
+    }
+  }
+  add_counter(&P.ctr->band, band_cnt);
+  add_counter(&P.ctr->ambiguous, amb_cnt);
+}
+
+// FP32 filter for d <= 32: the lane's candidate row lives in registers as DQ
+// float4 chunks (compile time), the home rows are visited in groups of 8 so
+// each shared-memory broadcast load feeds 8 independent FMA chains, and each
+// group is classified as soon as it is complete (8 live accumulators).
+template <int DQ>
+__global__ void __launch_bounds__(JOIN_THREADS, (DQ <= 4 ? 4 : 3))
+k_join_f32r(const JoinParams P) {
+  constexpr int CH = 32;
+  extern __shared__ float4 smem_f4r[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float4* sA = smem_f4r + (size_t)w * CH * DQ;
+  const float4* X = (const float4*)P.xs;
+  uint32_t band_cnt = 0, amb_cnt = 0;
+  for (;;) {
+    unsigned long long u = 0;
+    if (lane == 0) u = atomicAdd(&P.ctr->next_unit, 1ull);
+    u = __shfl_sync(FULL_MASK, u, 0);
+    if (u >= P.n_units) break;
+    const Unit U = P.units[u];
+    const uint32_t hs = P.bstart[U.h], he = P.bstart[U.h + 1];
+    const uint32_t a0 = hs + U.chunk * CH;
+    const uint32_t na = min((uint32_t)CH, he - a0);
+    __syncwarp();
+    for (uint32_t i = lane; i < CH * DQ; i += 32)
+      sA[i] = i < na * DQ ? X[(size_t)a0 * DQ + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
+    uint32_t s = U.s0, off = 0;
+    while (s < U.s1) {
+      const CandTile t = next_tile(P, s, off, U.s1);
+      const uint32_t q = t.q;
+      const float4* qrow = X + (size_t)(t.qv ? q : a0) * DQ;
+      float4 qq[DQ];
 #pragma unroll
-        for (int a = 0; a < CH; ++a) m |= (acc[a] <= P.t_hi ? 1u : 0u) << a;
-        m = qv ? (m & home_mask(na, self, q, a0, CH)) : 0u;
-        if (__any_sync(FULL_MASK, m != 0)) {
-          uint32_t lo_m = 0;
+      for (int c = 0; c < DQ; ++c) qq[c] = qrow[c];
+      uint32_t m = 0, lo_m = 0;
 #pragma unroll
-          for (int a = 0; a < CH; ++a) lo_m |= (acc[a] <= P.t_lo ? 1u : 0u) << a;
-          lo_m &= m;
-          uint32_t band = m & ~lo_m, acc_m = lo_m;
-          if (band) {
-            const uint32_t iq = P.ids[q];
-            while (band) {
-              const int a = __ffs(band) - 1;
-              band &= band - 1;
-              const double sd = exact_sqdist(P, P.ids[a0 + a], iq);
-              ++band_cnt;
-              if (fabs(sd - P.eps2) <= P.amb) ++amb_cnt;
-              if (sd <= P.eps2) acc_m |= 1u << a;
-            }
+      for (int g = 0; g < CH / 8; ++g) {
+        if (g * 8 >= (int)na) break;
+        float acc[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i] = 0.f;
+#pragma unroll
+        for (int c = 0; c < DQ; ++c) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const float4 aa = sA[(g * 8 + i) * DQ + c];
+            float tt;
+            tt = aa.x - qq[c].x; acc[i] = fmaf(tt, tt, acc[i]);
+            tt = aa.y - qq[c].y; acc[i] = fmaf(tt, tt, acc[i]);
+            tt = aa.z - qq[c].z; acc[i] = fmaf(tt, tt, acc[i]);
+            tt = aa.w - qq[c].w; acc[i] = fmaf(tt, tt, acc[i]);
           }
-          emit_pairs(P, acc_m, a0, q);
         }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          m |= (acc[i] <= P.t_hi ? 1u : 0u) << (g * 8 + i);
+          lo_m |= (acc[i] <= P.t_lo ? 1u : 0u) << (g * 8 + i);
+        }
+      }
+      m = t.qv ? (m & home_mask(na, q >= hs && q < he, q, a0, CH)) : 0u;
+      if (__any_sync(FULL_MASK, m != 0)) {
+        lo_m &= m;
+        uint32_t band = m & ~lo_m, acc_m = lo_m;
+        if (band) {
+          const uint32_t iq = P.ids[q];
+          while (band) {
+            const int a = __ffs(band) - 1;
+            band &= band - 1;
+            const double sd = exact_sqdist(P, P.ids[a0 + a], iq);
+            ++band_cnt;
+            if (fabs(sd - P.eps2) <= P.amb) ++amb_cnt;
+            if (sd <= P.eps2) acc_m |= 1u << a;
+          }
+        }
+        emit_pairs(P, acc_m, a0, q);
       }
     }
   }
@@ -182,6 +350,37 @@ k_join_f32(const JoinParams P) {
 }
 
 // ---------------------------------------------------------------- FP64 plain
+// The reference predicate for every candidate: dims in order, each
+// subtraction, product and sum rounded (no contraction).
+template <int CH>
+__device__ __forceinline__ void f64_dists(const double2* __restrict__ qrow, const double2* sA, uint32_t nq2,
+                                          uint32_t d, uint32_t na, double (&acc)[CH]) {
+  const uint32_t full = d >> 1;
+#pragma unroll
+  for (int a = 0; a < CH; ++a) acc[a] = 0.0;
+  for (uint32_t c = 0; c < full; ++c) {
+    const double2 qq = qrow[c];
+#pragma unroll
+    for (int a = 0; a < CH; ++a) {
+      if (a >= (int)na) break;
+      const double2 aa = sA[a * nq2 + c];
+      double t;
+      t = __dsub_rn(aa.x, qq.x); acc[a] = __dadd_rn(acc[a], __dmul_rn(t, t));
+      t = __dsub_rn(aa.y, qq.y); acc[a] = __dadd_rn(acc[a], __dmul_rn(t, t));
+    }
+  }
+  if (d & 1) {
+    const double2 qq = qrow[full];
+#pragma unroll
+    for (int a = 0; a < CH; ++a) {
+      if (a >= (int)na) break;
+      const double2 aa = sA[a * nq2 + full];
+      const double t = __dsub_rn(aa.x, qq.x);
+      acc[a] = __dadd_rn(acc[a], __dmul_rn(t, t));
+    }
+  }
+}
+
 template <int CH>
 __global__ void __launch_bounds__(JOIN_THREADS)
 k_join_f64(const JoinParams P) {
@@ -205,42 +404,30 @@ k_join_f64(const JoinParams P) {
     for (uint32_t i = lane; i < CH * nq2; i += 32)
       sA[i] = i < na * nq2 ? X[(size_t)a0 * nq2 + i] : make_double2(0.0, 0.0);
     __syncwarp();
-    for (uint32_t s = U.s0; s < U.s1; ++s) {
-      const uint32_t b = P.nbr[s];
-      const uint32_t q0 = P.bstart[b], q1 = P.bstart[b + 1];
-      const bool self = (b == U.h);
-      for (uint32_t qb = q0; qb < q1; qb += 32) {
-        const uint32_t q = qb + lane;
-        const bool qv = q < q1;
-        const double2* qrow = X + (size_t)(qv ? q : q0) * nq2;
-        double acc[CH];
+    uint32_t s = U.s0, off = 0;
+    while (s < U.s1) {
+      const CandTile t = next_tile(P, s, off, U.s1);
+      const uint32_t q = t.q;
+      const double2* qrow = X + (size_t)(t.qv ? q : a0) * nq2;
+      double acc[CH];
+      f64_dists<CH>(qrow, sA, nq2, P.d, na, acc);
+      uint32_t m = 0;
 #pragma unroll
-        for (int a = 0; a < CH; ++a) acc[a] = 0.0;
-        for (uint32_t c = 0; c < nq2; ++c) {
-          const double2 qq = qrow[c];
+      for (int a = 0; a < CH; ++a) {
+        if (a >= (int)na) break;
+        m |= (acc[a] <= thr ? 1u : 0u) << a;
+      }
+      m = t.qv ? (m & home_mask(na, q >= hs && q < he, q, a0, CH)) : 0u;
+      if (__any_sync(FULL_MASK, m != 0)) {
+        uint32_t acc_m = 0, amb_m = 0;
 #pragma unroll
-          for (int a = 0; a < CH; ++a) {
-            const double2 aa = sA[a * nq2 + c];
-            double t;
-            t = __dsub_rn(aa.x, qq.x); acc[a] = __dadd_rn(acc[a], __dmul_rn(t, t));
-            t = __dsub_rn(aa.y, qq.y); acc[a] = __dadd_rn(acc[a], __dmul_rn(t, t));
-          }
+        for (int a = 0; a < CH; ++a) {
+          acc_m |= (acc[a] <= P.eps2 ? 1u : 0u) << a;
+          amb_m |= (fabs(acc[a] - P.eps2) <= P.amb ? 1u : 0u) << a;
         }
-        uint32_t m = 0;
-#pragma unroll
-        for (int a = 0; a < CH; ++a) m |= (acc[a] <= thr ? 1u : 0u) << a;
-        m = qv ? (m & home_mask(na, self, q, a0, CH)) : 0u;
-        if (__any_sync(FULL_MASK, m != 0)) {
-          uint32_t acc_m = 0, amb_m = 0;
-#pragma unroll
-          for (int a = 0; a < CH; ++a) {
-            acc_m |= (acc[a] <= P.eps2 ? 1u : 0u) << a;
-            amb_m |= (fabs(acc[a] - P.eps2) <= P.amb ? 1u : 0u) << a;
-          }
-          acc_m &= m;
-          amb_cnt += __popc(amb_m & m);
-          emit_pairs(P, acc_m, a0, q);
-        }
+        acc_m &= m;
+        amb_cnt += __popc(amb_m & m);
+        emit_pairs(P, acc_m, a0, q);
       }
     }
   }
@@ -282,6 +469,18 @@ void run(mistic_handle_s* h, bool fp64, int CH, const JoinParams& P) {
   if (P.n_units == 0) return;
   if (!fp64) {
     const size_t spw = (size_t)CH * P.dpad * sizeof(float);
+    if (CH == 32 && P.dpad <= 32) {
+      switch (P.dpad / 4) {
+        case 1: launch_persistent(h, k_join_f32r<1>, spw, P, "join_f32r"); return;
+        case 2: launch_persistent(h, k_join_f32r<2>, spw, P, "join_f32r"); return;
+        case 3: launch_persistent(h, k_join_f32r<3>, spw, P, "join_f32r"); return;
+        case 4: launch_persistent(h, k_join_f32r<4>, spw, P, "join_f32r"); return;
+        case 5: launch_persistent(h, k_join_f32r<5>, spw, P, "join_f32r"); return;
+        case 6: launch_persistent(h, k_join_f32r<6>, spw, P, "join_f32r"); return;
+        case 7: launch_persistent(h, k_join_f32r<7>, spw, P, "join_f32r"); return;
+        default: launch_persistent(h, k_join_f32r<8>, spw, P, "join_f32r"); return;
+      }
+    }
     if (CH == 32)
       launch_persistent(h, k_join_f32<32>, spw, P, "join_f32");
     else
