@@ -318,7 +318,8 @@ def run_mistic(args, wl) -> None:
         "band_fraction": r.band_pairs / max(1, r.candidates),
         "distance_evals_per_s": r.candidates / (ms * 1e-3), "pairs_per_s": r.pairs_ij / (ms * 1e-3),
         "phase_ms": {k: round(v, 3) for k, v in r.ms.items()},
-        "bins": r.n_bins, "bin_pairs": r.n_bin_pairs, "units": r.n_units, "k_used": r.k_used,
+        "bins": r.n_bins, "bin_pairs": r.n_bin_pairs, "units": r.n_units, "units_tc": r.n_units_tc,
+        "k_used": r.k_used,
         "fp64_plain": fp64,
         "roofline": {"bound": "fp32", "kernel": "k_join_f32", "achieved": achieved,
                      "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None,

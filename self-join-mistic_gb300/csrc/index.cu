@@ -307,14 +307,19 @@ __device__ __forceinline__ uint32_t lower_bound_u64(const uint64_t* __restrict__
 template <bool FILL>
 __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __restrict__ bstart,
                        uint32_t m, EnumParams P, uint32_t* __restrict__ nbr_cnt,
-                       uint32_t* __restrict__ unit_cnt, unsigned long long* __restrict__ cand,
-                       const uint32_t* __restrict__ nbr_off, const uint32_t* __restrict__ unit_off,
-                       uint32_t* __restrict__ nbr, Unit* __restrict__ units) {
+                       uint32_t* __restrict__ unit_cnt, uint32_t* __restrict__ unit_cnt_tc,
+                       unsigned long long* __restrict__ cand, const uint32_t* __restrict__ nbr_off,
+                       const uint32_t* __restrict__ unit_off, const uint32_t* __restrict__ unit_off_tc,
+                       uint32_t* __restrict__ nbr, Unit* __restrict__ units_simt, Unit* __restrict__ units_tc) {
   const uint32_t hb = blockIdx.x * blockDim.x + threadIdx.x;
   if (hb >= m) return;
   const uint64_t K = bkey[hb];
   const uint32_t asz = bstart[hb + 1] - bstart[hb];
-  const uint32_t nchunks = (asz + P.chunk - 1) / P.chunk;
+  // large home bins go to the tensor-core join (128-row chunks), the rest to the CUDA-core join
+  const bool tc = P.tc_min > 0 && asz >= P.tc_min;
+  const uint32_t csz = tc ? P.tc_chunk : P.chunk;
+  const uint32_t nchunks = (asz + csz - 1) / csz;
+  Unit* __restrict__ units = tc ? units_tc : units_simt;
 
   int kf[MAX_K];
   // decode fields: field j spans [shift[j], shift[j-1]) (shift[-1] = 64)
@@ -337,7 +342,7 @@ __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __rest
   uint32_t cnt = 0, nseg = 0, seg_fill = 0, seg_begin = 0;
   unsigned long long c = 0;
   uint32_t w_nbr = FILL ? nbr_off[hb] : 0;
-  uint32_t w_unit = FILL ? unit_off[hb] : 0;
+  uint32_t w_unit = FILL ? (tc ? unit_off_tc[hb] : unit_off[hb]) : 0;
 
   // Visits neighbour bin `a` (ascending, a >= hb): candidate count, segment
   // split and, in pass 2, the neighbour list and the units.
@@ -401,7 +406,8 @@ __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __rest
   }
   if (!FILL) {
     nbr_cnt[hb] = cnt;
-    unit_cnt[hb] = nseg * nchunks;
+    unit_cnt[hb] = tc ? 0u : nseg * nchunks;
+    unit_cnt_tc[hb] = tc ? nseg * nchunks : 0u;
     cand[hb] = c;
   }
 }
@@ -489,15 +495,16 @@ void gather(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, uint32
 }
 
 void enumerate(mistic_handle_s* h, const uint64_t* bkey, const uint32_t* bstart, uint32_t m,
-               const EnumParams& P, uint32_t* nbr_cnt, uint32_t* unit_cnt, unsigned long long* cand,
-               const uint32_t* nbr_off, const uint32_t* unit_off, uint32_t* nbr, Unit* units, bool fill) {
+               const EnumParams& P, uint32_t* nbr_cnt, uint32_t* unit_cnt, uint32_t* unit_cnt_tc,
+               unsigned long long* cand, const uint32_t* nbr_off, const uint32_t* unit_off,
+               const uint32_t* unit_off_tc, uint32_t* nbr, Unit* units, Unit* units_tc, bool fill) {
   const unsigned nb = (m + 127) / 128;
   if (!fill)
-    k_enum<false><<<nb, 128, 0, h->stream>>>(bkey, bstart, m, P, nbr_cnt, unit_cnt, cand, nullptr, nullptr,
-                                             nullptr, nullptr);
+    k_enum<false><<<nb, 128, 0, h->stream>>>(bkey, bstart, m, P, nbr_cnt, unit_cnt, unit_cnt_tc, cand, nullptr,
+                                             nullptr, nullptr, nullptr, nullptr, nullptr);
   else
-    k_enum<true><<<nb, 128, 0, h->stream>>>(bkey, bstart, m, P, nullptr, nullptr, nullptr, nbr_off, unit_off,
-                                            nbr, units);
+    k_enum<true><<<nb, 128, 0, h->stream>>>(bkey, bstart, m, P, nullptr, nullptr, nullptr, nullptr, nbr_off,
+                                            unit_off, unit_off_tc, nbr, units, units_tc);
   launched(h, fill ? "enum_fill" : "enum_count");
 }
 

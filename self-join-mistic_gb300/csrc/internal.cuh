@@ -74,6 +74,7 @@ struct JoinCounters {
   unsigned long long band;       // pairs re-decided in FP64
   unsigned long long ambiguous;  // FP64 value within 4 ulp of eps2
   unsigned long long next_unit;  // work-queue cursor
+  unsigned long long error;      // non-zero: a bounded device wait gave up
 };
 
 // Key packing: field f = floor((D[i*kstride + col[f]] - dmin[f]) / w[f]),
@@ -94,7 +95,9 @@ struct EnumParams {
   int shift[MAX_K];
   uint32_t maxkey[MAX_K];
   uint32_t seg_cap;  // candidate points per neighbour segment
-  uint32_t chunk;    // home points per unit
+  uint32_t chunk;    // home points per CUDA-core unit
+  uint32_t tc_min;   // home bins with at least this many points get tensor-core units (0: none)
+  uint32_t tc_chunk; // home points per tensor-core unit
 };
 
 struct JoinParams {
@@ -114,6 +117,20 @@ struct JoinParams {
   unsigned long long* pairs;  // packed (i << 32 | j), i < j; null when counting only
   unsigned long long cap;
   JoinCounters* ctr;
+};
+
+// Tensor-core join: FP32 constants of the per-row error bound (see join_tc.cu).
+struct TcParams {
+  const Unit* units;
+  unsigned long long n_units;
+  JoinCounters* ctr;  // separate cursor from the CUDA-core join
+  float eps2_lo, eps2_hi;  // fl32 bounds of eps2/(1+g64), eps2/(1-g64)
+  float kappa;             // relative MMA + norm error per (|a'|+|q'|)^2
+  float ginf;              // norm inflation 1/(1-g_d)
+  float uR2;               // 2uR (global centring error)
+  float u1;                // u(1+u)
+  float Dp;                // 1.1 sqrt(eps2)
+  float cap;               // 0.1 eps2: larger bounds re-decide the whole row in FP64
 };
 
 struct Timer {
@@ -169,20 +186,24 @@ void gather(mistic_handle_s*, const void* x, mistic_dtype, size_t n, uint32_t d,
             const double* center, uint32_t dpad32, float* xf, uint32_t dpad64, double* xd,
             uint32_t* ids, double* norm_part, double* rmax);
 void enumerate(mistic_handle_s*, const uint64_t* bkey, const uint32_t* bstart, uint32_t m,
-               const EnumParams&, uint32_t* nbr_cnt, uint32_t* unit_cnt, unsigned long long* cand,
-               const uint32_t* nbr_off, const uint32_t* unit_off, uint32_t* nbr, Unit* units,
-               bool fill);
+               const EnumParams&, uint32_t* nbr_cnt, uint32_t* unit_cnt, uint32_t* unit_cnt_tc,
+               unsigned long long* cand, const uint32_t* nbr_off, const uint32_t* unit_off,
+               const uint32_t* unit_off_tc, uint32_t* nbr, Unit* units, Unit* units_tc, bool fill);
 }  // namespace idx
 
 // ---- mistic.cu: FP32 filter thresholds (accept at or below t_lo, re-decide
 // in FP64 above it up to t_hi) for dimension d, eps2 = fl(ε*ε) and largest
-// centred FP32 row norm R.
-void filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_hi);
+// centred FP32 row norm R; false when FP32 cannot separate pairs at this ε.
+bool filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_hi);
 
 // ---- join.cu
 namespace join {
 int chunk_for(bool fp64, uint32_t dpad);
 void run(mistic_handle_s*, bool fp64, int CH, const JoinParams&);
+// Tensor-core join over TcParams.units; KP = augmented K (d + 2 rounded up to 16).
+bool tc_supported(uint32_t d);
+int tc_kp(uint32_t d);
+void run_tc(mistic_handle_s*, const JoinParams&, const TcParams&);
 }  // namespace join
 
 // ---- rp.cpp: reference-point selection on the host.

@@ -15,6 +15,7 @@
 // The host synchronises only for a handful of scalars (key layout, bin and
 // work-list sizes, final counts).
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -82,18 +83,22 @@ void Arena::release_all() {
 // largest ||x~||, u = 2^-24 (inflated for the FP64 centring), the error is
 //   |s32 - D^2| <= E(D) = (1+g_d)(2u(2R+D)D + u^2(2R+D)^2) + g_d D^2 + tiny,
 // g_d = d u / (1 - d u).  The reference value s64 (sequential FP64) obeys
-// |s64 - D^2| <= g64 D^2.  With D' = 1.01 sqrt(eps2), every pair with
-// s32 <= T_lo = eps2/(1+g64) - E(D') has s64 <= eps2, and every pair with
-// s32 > T_hi = eps2/(1-g64) + E(D') has s64 > eps2 (E grows slower than D^2,
-// so pairs with D > D' are beyond T_hi as well); pairs between are re-decided.
-void filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_hi) {
+// |s64 - D^2| <= g64 D^2.  With D' = 1.1 sqrt(eps2) and E' = E(D'), every
+// pair with s32 <= T_lo = eps2/(1+g64) - E' has s64 <= eps2, and every pair
+// with s32 > T_hi = eps2/(1-g64) + E' has s64 > eps2: for D <= D' directly,
+// and for D > D' because D^2 - E(D) grows with D and already exceeds T_hi at
+// D' whenever E' <= 0.1 eps2.  Returns false when that condition fails (the
+// coordinates are too large relative to ε for FP32); the caller then joins
+// in FP64.
+bool filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_hi) {
   const double u = ldexp(1.0, -24) * (1.0 + ldexp(1.0, -20));
   const double gd = d * u / (1.0 - d * u);
   const double g64 = (d + 2) * ldexp(1.0, -53) * 1.01;
-  const double Dp = 1.01 * sqrt(eps2);
+  const double Dp = 1.1 * sqrt(eps2);
   const double tiny = (double)(d + 2) * ldexp(1.0, -126);
   const double E = (1.0 + gd) * (2.0 * u * (2.0 * R + Dp) * Dp + u * u * (2.0 * R + Dp) * (2.0 * R + Dp)) +
                    gd * Dp * Dp + tiny;
+  if (!(E <= 0.1 * eps2)) return false;
   double lo = eps2 / (1.0 + g64) - E;
   double hi = eps2 / (1.0 - g64) + E;
   lo *= 1.0 - 1e-12;
@@ -104,6 +109,7 @@ void filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_
   if ((double)fhi < hi) fhi = nextafterf(fhi, INFINITY);
   *t_lo = flo;
   *t_hi = fhi;
+  return true;
 }
 
 namespace {
@@ -146,6 +152,14 @@ int bit_length(uint64_t v) {
   return b;
 }
 
+// Smallest home bin that goes to the tensor-core join.  MISTIC_TC_MIN_BIN
+// overrides it (tuning).
+uint32_t tc_min_bin() {
+  const char* e = getenv("MISTIC_TC_MIN_BIN");
+  if (e && *e) return (uint32_t)std::max(1l, strtol(e, nullptr, 10));
+  return 16;
+}
+
 void check_handle(mistic_handle h) {
   if (!h) throw Error(MISTIC_ERR_INVALID_ARG, "null handle");
   MCK(cudaSetDevice(h->device));
@@ -173,7 +187,8 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   if (k > MAX_K) throw Error(MISTIC_ERR_INVALID_ARG, "k above the supported maximum (16)");
   if (n >= 0xffffffffull) throw Error(MISTIC_ERR_TOO_LARGE, "n must be below 2^32 - 1");
   if (n > 0 && !pts) throw Error(MISTIC_ERR_INVALID_ARG, "null points");
-  if (o.mode != MISTIC_MODE_AUTO && o.mode != MISTIC_MODE_FP64 && o.mode != MISTIC_MODE_FP32)
+  if (o.mode != MISTIC_MODE_AUTO && o.mode != MISTIC_MODE_FP64 && o.mode != MISTIC_MODE_FP32 &&
+      o.mode != MISTIC_MODE_BF16)
     throw Error(MISTIC_ERR_INVALID_ARG, "unknown mode");
   if (o.pairs != MISTIC_PAIRS_NONE && o.pairs != MISTIC_PAIRS_HOST && o.pairs != MISTIC_PAIRS_DEVICE)
     throw Error(MISTIC_ERR_INVALID_ARG, "unknown pairs destination");
@@ -347,40 +362,50 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   if (!fp64) {
     // FP32 range guard: fall back to the FP64 join when FP32 cannot hold the
     // coordinates or ε² comfortably.
-    if (R > 1e15 || (eps2 > 0 && eps2 < 1e-28) || eps2 == 0.0) {
+    if (R > 1e15 || (eps2 > 0 && eps2 < 1e-28) || eps2 == 0.0 ||
+        !filter_thresholds(d, eps2, R, &t_lo, &t_hi)) {
       fp64 = true;
       xd = abuf<double>(h, "xd", n * dpad64);
       idx::gather(h, x, dt, n, d, perm, dcenter, 0, nullptr, dpad64, xd, ids, npart, rmax);
-    } else {
-      filter_thresholds(d, eps2, R, &t_lo, &t_hi);
     }
   }
-  r->mode_used = fp64 ? MISTIC_MODE_FP64 : MISTIC_MODE_FP32;
+  // tensor cores for large home bins when the FP32 view is usable and the
+  // augmented K fits one operand tile
+  const bool use_tc = !fp64 && o.mode == MISTIC_MODE_BF16 && join::tc_supported(d) && eps2 > 1e-20;
+  r->mode_used = fp64 ? MISTIC_MODE_FP64 : (use_tc ? MISTIC_MODE_BF16 : MISTIC_MODE_FP32);
   clk.mark();  // 5
 
   // ---- neighbour enumeration -> work units
   const int CH = join::chunk_for(fp64, fp64 ? dpad64 : dpad32);
   ep.chunk = (uint32_t)CH;
   ep.seg_cap = 4096;
+  ep.tc_min = use_tc ? tc_min_bin() : 0u;
+  ep.tc_chunk = 128;
   uint32_t* nbr_cnt = abuf<uint32_t>(h, "nbr_cnt", m + 1);
   uint32_t* unit_cnt = abuf<uint32_t>(h, "unit_cnt", m + 1);
+  uint32_t* unit_cnt_tc = abuf<uint32_t>(h, "unit_cnt_tc", m + 1);
   unsigned long long* cand = abuf<unsigned long long>(h, "cand", m + 1);
-  idx::enumerate(h, bkey, bstart, m, ep, nbr_cnt, unit_cnt, cand, nullptr, nullptr, nullptr, nullptr, false);
-  uint32_t* tot32 = abuf<uint32_t>(h, "tot32", 2);
+  idx::enumerate(h, bkey, bstart, m, ep, nbr_cnt, unit_cnt, unit_cnt_tc, cand, nullptr, nullptr, nullptr, nullptr,
+                 nullptr, nullptr, false);
+  uint32_t* tot32 = abuf<uint32_t>(h, "tot32", 3);
   unsigned long long* tot64 = abuf<unsigned long long>(h, "tot64", 1);
   exclusive_scan<uint32_t>(h, nbr_cnt, nbr_cnt, m, tot32);
   exclusive_scan<uint32_t>(h, unit_cnt, unit_cnt, m, tot32 + 1);
+  exclusive_scan<uint32_t>(h, unit_cnt_tc, unit_cnt_tc, m, tot32 + 2);
   exclusive_scan<unsigned long long>(h, cand, cand, m, tot64);
-  uint32_t tots[2];
+  uint32_t tots[3];
   unsigned long long totc = 0;
   d2h(h, tots, tot32, sizeof tots);
   d2h(h, &totc, tot64, sizeof totc);
   r->n_bin_pairs = tots[0];
   r->n_units = tots[1];
+  r->n_units_tc = tots[2];
   r->candidates = totc;
   uint32_t* nbr = abuf<uint32_t>(h, "nbr", (size_t)tots[0] + 1);
   Unit* units = abuf<Unit>(h, "units", (size_t)tots[1] + 1);
-  idx::enumerate(h, bkey, bstart, m, ep, nullptr, nullptr, nullptr, nbr_cnt, unit_cnt, nbr, units, true);
+  Unit* units_tc = abuf<Unit>(h, "units_tc", (size_t)tots[2] + 1);
+  idx::enumerate(h, bkey, bstart, m, ep, nullptr, nullptr, nullptr, nullptr, nbr_cnt, unit_cnt, unit_cnt_tc, nbr,
+                 units, units_tc, true);
   clk.mark();  // 6
 
   // ---- join
@@ -399,7 +424,27 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   jp.t_hi = t_hi;
   jp.eps2 = eps2;
   jp.amb = 4.0 * (nextafter(eps2, INFINITY) - eps2);
-  JoinCounters* ctr = abuf<JoinCounters>(h, "ctr", 1);
+  JoinCounters* ctr = abuf<JoinCounters>(h, "ctr", 2);  // [0] CUDA-core join, [1] tensor-core cursor
+  TcParams tp{};
+  if (use_tc) {
+    const double u = ldexp(1.0, -24) * (1.0 + ldexp(1.0, -20));
+    const double gd = d * u / (1.0 - d * u);
+    const double g64 = (d + 2) * ldexp(1.0, -53) * 1.01;
+    const int n_mma = 3 * join::tc_kp(d) / 16;
+    tp.units = units_tc;
+    tp.n_units = tots[2];
+    tp.ctr = ctr + 1;
+    tp.eps2_lo = (float)(eps2 / (1.0 + g64));
+    if ((double)tp.eps2_lo > eps2 / (1.0 + g64)) tp.eps2_lo = nextafterf(tp.eps2_lo, 0.f);
+    tp.eps2_hi = (float)(eps2 / (1.0 - g64));
+    if ((double)tp.eps2_hi < eps2 / (1.0 - g64)) tp.eps2_hi = nextafterf(tp.eps2_hi, INFINITY);
+    tp.kappa = (float)((3.02 * ldexp(1.0, -18) + n_mma * ldexp(1.0, -19) + gd) * (1.0 + gd) * 1.01);
+    tp.ginf = (float)(1.0 / (1.0 - gd) * (1.0 + 1e-6));
+    tp.uR2 = (float)(2.0 * u * R * 1.0001);
+    tp.u1 = (float)(u * (1.0 + u) * 1.0001);
+    tp.Dp = (float)(1.1 * sqrt(eps2));
+    tp.cap = (float)(0.1 * eps2);
+  }
   const bool want_pairs = o.pairs != MISTIC_PAIRS_NONE;
   unsigned long long cap = 0;
   unsigned long long* pbuf = nullptr;
@@ -420,9 +465,11 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   jp.ctr = ctr;
   JoinCounters hc{};
   for (int attempt = 0; attempt < 2; ++attempt) {
-    MCK(cudaMemsetAsync(ctr, 0, sizeof(JoinCounters), h->stream));
+    MCK(cudaMemsetAsync(ctr, 0, 2 * sizeof(JoinCounters), h->stream));
     join::run(h, fp64, CH, jp);
+    if (use_tc) join::run_tc(h, jp, tp);
     d2h(h, &hc, ctr, sizeof hc);
+    if (hc.error) throw Error(MISTIC_ERR_TIMEOUT, "a tensor-core tile wait timed out");
     if (!want_pairs || hc.pairs <= cap || o.pair_capacity) break;
     cap = hc.pairs;
     pbuf = abuf<unsigned long long>(h, "pairs", cap);

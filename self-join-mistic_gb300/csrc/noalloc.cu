@@ -279,11 +279,9 @@ extern "C" mistic_status mistic_selfjoin_noalloc(const void* d_pts, uint64_t n, 
   memcpy(&r2, &hh.r2max_bits, sizeof r2);
   const double R = sqrt(r2) * (1.0 + 1e-12);
   const double eps2 = P.eps2;
-  if (eps2 == 0.0 || eps2 < 1e-28 || R > 1e15) {
+  if (eps2 == 0.0 || eps2 < 1e-28 || R > 1e15 || !filter_thresholds(d, eps2, R, &P.t_lo, &P.t_hi)) {
     P.t_lo = -1.0f;  // FP32 cannot separate these pairs: re-decide every candidate in FP64
     P.t_hi = INFINITY;
-  } else {
-    filter_thresholds(d, eps2, R, &P.t_lo, &P.t_hi);
   }
   const uint32_t nchunks = (uint32_t)((n + kCH - 1) / kCH);
   P.nseg = (uint32_t)((n + kSeg - 1) / kSeg);

@@ -19,7 +19,7 @@ from . import _lib as L
 
 __all__ = ["MisticError", "JoinResult", "Handle", "selfjoin", "read_points"]
 
-MODES = {"auto": L.MODE_AUTO, "fp64": L.MODE_FP64, "fp32": L.MODE_FP32}
+MODES = {"auto": L.MODE_AUTO, "fp64": L.MODE_FP64, "fp32": L.MODE_FP32, "bf16": L.MODE_BF16}
 RP_MODES = {"pca": L.RP_PCA, "box": L.RP_BOX, "user": L.RP_USER}
 
 
@@ -42,6 +42,7 @@ class JoinResult:
     n_bins: int
     n_bin_pairs: int
     n_units: int
+    n_units_tc: int
     mode_used: str
     ms: dict
     kernel_launches: int
@@ -131,8 +132,8 @@ class Handle:
             n=r.n, d=r.d, k_used=r.k_used, pairs_ij=r.pairs_ij,
             pairs_ordered_incl_self=r.pairs_ordered_incl_self, candidates=r.candidates,
             band_pairs=r.band_pairs, ulp_ambiguous=r.ulp_ambiguous, n_bins=r.n_bins,
-            n_bin_pairs=r.n_bin_pairs, n_units=r.n_units,
-            mode_used={0: "auto", 1: "fp64", 2: "fp32"}.get(r.mode_used, "?"),
+            n_bin_pairs=r.n_bin_pairs, n_units=r.n_units, n_units_tc=r.n_units_tc,
+            mode_used={0: "auto", 1: "fp64", 2: "fp32", 3: "bf16"}.get(r.mode_used, "?"),
             ms=ms, kernel_launches=r.kernel_launches, pairs=pairs, device_pairs=dev)
         if not keep_device or not r.pairs_on_device:
             self.lib.mistic_result_free(ctypes.byref(r))

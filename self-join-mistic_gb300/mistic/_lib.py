@@ -20,7 +20,7 @@ ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_TOO_LARGE = 1, 2, 3, 4
 ERR_NOT_FINITE, ERR_PAIR_OVERFLOW, ERR_TIMEOUT, ERR_NO_DEVICE = 5, 6, 7, 8
 ERR_IO, ERR_INTERNAL = 9, 10
 F64, F32 = 0, 1
-MODE_AUTO, MODE_FP64, MODE_FP32 = 0, 1, 2
+MODE_AUTO, MODE_FP64, MODE_FP32, MODE_BF16 = 0, 1, 2, 3
 RP_PCA, RP_BOX, RP_USER = 0, 1, 2
 PAIRS_NONE, PAIRS_HOST, PAIRS_DEVICE = 0, 1, 2
 
@@ -66,6 +66,7 @@ class Result(ctypes.Structure):
         ("n_bins", u64),
         ("n_bin_pairs", u64),
         ("n_units", u64),
+        ("n_units_tc", u64),
         ("pairs", ctypes.POINTER(u32)),
         ("pairs_len", u64),
         ("pairs_on_device", i32),

@@ -12,7 +12,7 @@ from mistic import _lib as L
 
 pytestmark = pytest.mark.gpu
 
-MODES = ["auto", "fp64", "fp32"]
+MODES = ["auto", "fp64", "fp32", "bf16"]
 
 
 def run(h, x, k, eps, **kw):
@@ -67,6 +67,24 @@ def test_medium_uniform18(handle, mode):
     r = run(handle, x, 6, eps, mode=mode)
     assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)
     assert r.candidates >= r.pairs_ij
+
+
+@pytest.mark.parametrize("tc_min", ["1", "16", "100000"])
+def test_tensor_core_split_points(handle, monkeypatch, tc_min):
+    """Every home bin on the tensor cores (1), the default split (16), none (huge)."""
+    monkeypatch.setenv("MISTIC_TC_MIN_BIN", tc_min)
+    from mistic import workloads as W
+    for x, k, eps in ((W.gen_susy_like(30000, seed=6), 6, 0.03),
+                      (np.random.default_rng(4).normal(size=(6000, 90)), 8, 9.0),
+                      (np.random.default_rng(5).random((5000, 3)), 3, 0.02)):
+        ref = O.brute_pairs(x, eps)
+        r = run(handle, x, k, eps, mode="bf16")
+        assert r.mode_used == "bf16"
+        if tc_min == "1":
+            assert r.n_units == 0 and r.n_units_tc > 0
+        if tc_min == "100000":
+            assert r.n_units_tc == 0
+        assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)
 
 
 def test_modes_agree_and_band_is_small(handle):
