@@ -227,10 +227,11 @@ def run_mistic(args, wl) -> None:
 
     # first call sizes the caller-owned device pair buffer
     r0 = h.to_result(h.selfjoin_raw(xt.data_ptr(), n, d, dt, wl.k, wl.eps,
-                                    h.opts(input_on_device=True)))
+                                    h.opts(input_on_device=True, mode=args.mode)))
     cap = int(r0.pairs_ij * 1.02) + 1024
     pbuf = torch.empty((cap,), dtype=torch.int64, device=dev)
-    o_dev = h.opts(input_on_device=True, pairs="device", pair_capacity=cap, pair_buffer=pbuf.data_ptr())
+    o_dev = h.opts(input_on_device=True, pairs="device", pair_capacity=cap, pair_buffer=pbuf.data_ptr(),
+                   mode=args.mode)
 
     def step(opts):
         return h.to_result(h.selfjoin_raw(xt.data_ptr(), n, d, dt, wl.k, wl.eps, opts))
@@ -259,7 +260,7 @@ def run_mistic(args, wl) -> None:
     launches = sum(q.kernel_launches for q in results)
 
     # ---- e2e: host input, host pair list, through the same C ABI call
-    o_host = h.opts(pairs="host")
+    o_host = h.opts(pairs="host", mode=args.mode)
     for _ in range(1):
         h.to_result(h.selfjoin_raw(x.ctypes.data, n, d, dt, wl.k, wl.eps, o_host))
     barrier()
@@ -277,7 +278,7 @@ def run_mistic(args, wl) -> None:
     if not args.no_fp64:
         pb2 = torch.empty_like(pbuf)
         o_s = h.opts(input_on_device=True, pairs="device", pair_capacity=cap, pair_buffer=pbuf.data_ptr(),
-                     sort_pairs=True)
+                     sort_pairs=True, mode=args.mode)
         o_f = h.opts(input_on_device=True, pairs="device", pair_capacity=cap, pair_buffer=pb2.data_ptr(),
                      sort_pairs=True, mode="fp64")
         rs = step(o_s)
@@ -319,6 +320,7 @@ def run_mistic(args, wl) -> None:
         "distance_evals_per_s": r.candidates / (ms * 1e-3), "pairs_per_s": r.pairs_ij / (ms * 1e-3),
         "phase_ms": {k: round(v, 3) for k, v in r.ms.items()},
         "bins": r.n_bins, "bin_pairs": r.n_bin_pairs, "units": r.n_units, "units_tc": r.n_units_tc,
+        "tc_tiles": r.tc_tiles, "tc_fill": r.tc_cells / max(1, r.tc_tiles * 128 * 128),
         "k_used": r.k_used,
         "fp64_plain": fp64,
         "roofline": {"bound": "fp32", "kernel": "k_join_f32", "achieved": achieved,
@@ -366,6 +368,8 @@ def main() -> None:
     ap.add_argument("--impl", choices=["mistic", "reference"], default="mistic")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="susy18")
     ap.add_argument("--n", type=int, default=0, help="override the point count (testing)")
+    ap.add_argument("--mode", choices=["auto", "fp32", "bf16", "fp64"], default="auto",
+                    help="join mode of the timed steps")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

@@ -68,7 +68,7 @@ typedef enum mistic_dtype {
 } mistic_dtype;
 
 typedef enum mistic_mode {
-  MISTIC_MODE_AUTO = 0, /* the fastest exact mode measured for d (currently the FP32 filter) */
+  MISTIC_MODE_AUTO = 0, /* BF16 tensor-core mode for 8 <= d <= 126, else the FP32 filter */
   MISTIC_MODE_FP64 = 1, /* plain FP64 CUDA-core distances for every candidate */
   MISTIC_MODE_FP32 = 2, /* FP32 CUDA-core filter + FP64 re-decision of the band */
   MISTIC_MODE_BF16 = 3  /* large home bins as split-BF16 tensor-core Gram tiles (FP32
@@ -119,6 +119,8 @@ typedef struct mistic_result {
   uint64_t n_bin_pairs;             /* (home bin, neighbour bin) work items, home <= neighbour */
   uint64_t n_units;                 /* CUDA-core join work units after splitting */
   uint64_t n_units_tc;              /* tensor-core join work units (128-row home chunks) */
+  uint64_t tc_tiles;                /* 128 x 128 tensor-core tiles evaluated */
+  uint64_t tc_cells;                /* their occupied (home row, candidate) cells */
   uint32_t* pairs;                  /* 2*pairs_ij uint32 (i, j), i < j, or NULL */
   uint64_t pairs_len;               /* pairs stored (== pairs_ij unless capped) */
   int32_t pairs_on_device;

@@ -1,0 +1,79 @@
+// Warp-level staging of result pairs, shared by the join kernels.
+//
+// A warp collects accepted pairs in a small shared-memory buffer and
+// reserves space in the global pair list once per flush (one atomicAdd per
+// up to PSTAGE pairs, then coalesced stores), instead of one atomicAdd per
+// tile that holds a hit: the pair counter is a single address that every SM
+// updates, so per-tile atomics serialise in L2.  The reference appends every
+// pair with its own 64-bit atomicAdd (src/kernel.cu:1040-1043).
+#pragma once
+
+#include "internal.cuh"
+
+namespace mistic {
+
+constexpr uint32_t PSTAGE = 64;
+
+struct PairStage {
+  unsigned long long* buf;  // this warp's PSTAGE slots in shared memory
+  uint32_t n;               // staged pairs (warp-uniform)
+};
+
+__device__ __forceinline__ uint32_t stage_scan(uint32_t x) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(FULL_MASK, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
+// Warp-collective: moves the staged pairs to the global list.
+__device__ __forceinline__ void stage_flush(PairStage& ps, unsigned long long* counter,
+                                            unsigned long long* pairs, unsigned long long cap) {
+  if (ps.n == 0) return;
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(counter, (unsigned long long)ps.n);
+  base = __shfl_sync(FULL_MASK, base, 0);
+  if (pairs) {
+    for (uint32_t i = lane; i < ps.n; i += 32) {
+      const unsigned long long pos = base + i;
+      if (pos < cap) pairs[pos] = ps.buf[i];
+    }
+  }
+  __syncwarp();
+  ps.n = 0;
+}
+
+// Warp-collective: adds this lane's `cnt` pairs, produced in order by
+// `pair_of(k)` for k = 0..cnt-1 (packed (i << 32 | j), i < j).
+template <class F>
+__device__ __forceinline__ void stage_pairs(PairStage& ps, uint32_t cnt, F pair_of, unsigned long long* counter,
+                                            unsigned long long* pairs, unsigned long long cap) {
+  const uint32_t incl = stage_scan(cnt);
+  const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+  if (total == 0) return;
+  if (ps.n + total > PSTAGE) stage_flush(ps, counter, pairs, cap);
+  if (total > PSTAGE) {  // a dense block: reserve directly
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == 31) base = atomicAdd(counter, (unsigned long long)total);
+    base = __shfl_sync(FULL_MASK, base, 31);
+    if (pairs) {
+      unsigned long long pos = base + incl - cnt;
+      for (uint32_t k = 0; k < cnt; ++k, ++pos)
+        if (pos < cap) pairs[pos] = pair_of(k);
+    }
+    return;
+  }
+  if (pairs) {
+    uint32_t pos = ps.n + incl - cnt;
+    for (uint32_t k = 0; k < cnt; ++k) ps.buf[pos + k] = pair_of(k);
+  }
+  __syncwarp();
+  ps.n += total;
+}
+
+}  // namespace mistic

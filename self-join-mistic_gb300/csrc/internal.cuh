@@ -75,6 +75,8 @@ struct JoinCounters {
   unsigned long long ambiguous;  // FP64 value within 4 ulp of eps2
   unsigned long long next_unit;  // work-queue cursor
   unsigned long long error;      // non-zero: a bounded device wait gave up
+  unsigned long long tiles;      // tensor-core tiles evaluated
+  unsigned long long cells;      // sum over those tiles of home rows x candidate columns
 };
 
 // Key packing: field f = floor((D[i*kstride + col[f]] - dmin[f]) / w[f]),
@@ -130,7 +132,8 @@ struct TcParams {
   float uR2;               // 2uR (global centring error)
   float u1;                // u(1+u)
   float Dp;                // 1.1 sqrt(eps2)
-  float cap;               // 0.1 eps2: larger bounds re-decide the whole row in FP64
+  float cap;               // 0.1 eps2: larger bounds re-decide the whole column in FP64
+  float margin;            // small positive slack that makes D' >= 0 a strict reject
 };
 
 struct Timer {

@@ -23,7 +23,10 @@
 #include <math.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 
+#include "emit.cuh"
 #include "internal.cuh"
 
 namespace mistic {
@@ -62,29 +65,22 @@ __device__ __forceinline__ double exact_sqdist(const JoinParams& P, uint32_t i, 
   return s;
 }
 
-// Emits the accepted pairs of one lane (bit a of `acc` = home point a0 + a
-// paired with candidate q), one atomicAdd per warp.
-__device__ __forceinline__ void emit_pairs(const JoinParams& P, uint32_t acc, uint32_t a0, uint32_t q) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t cnt = __popc(acc);
-  const uint32_t incl = warp_incl_scan_u32(cnt);
-  const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
-  if (total == 0) return;
-  unsigned long long base = 0;
-  if (lane == 31) base = atomicAdd(&P.ctr->pairs, (unsigned long long)total);
-  base = __shfl_sync(FULL_MASK, base, 31);
-  if (P.pairs && cnt) {
-    unsigned long long pos = base + incl - cnt;
-    const uint32_t iq = P.ids[q];
-    while (acc) {
-      const int a = __ffs(acc) - 1;
-      acc &= acc - 1;
-      const uint32_t ia = P.ids[a0 + a];
-      const uint32_t lo = ia < iq ? ia : iq, hi = ia < iq ? iq : ia;
-      if (pos < P.cap) P.pairs[pos] = ((unsigned long long)lo << 32) | hi;
-      ++pos;
-    }
-  }
+// Stages this lane's accepted pairs (bit a of `acc`: home point a0 + a with
+// candidate q) through the warp's buffer.
+__device__ __forceinline__ void stage_hits(PairStage& ps, const JoinParams& P, uint32_t acc, uint32_t a0,
+                                           uint32_t q) {
+  const uint32_t iq = acc ? P.ids[q] : 0u;
+  uint32_t bits = acc;
+  stage_pairs(
+      ps, __popc(acc),
+      [&](uint32_t) {
+        const int a = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const uint32_t ia = P.ids[a0 + a];
+        const uint32_t lo = ia < iq ? ia : iq, hi = ia < iq ? iq : ia;
+        return ((unsigned long long)lo << 32) | hi;
+      },
+      &P.ctr->pairs, P.pairs, P.cap);
 }
 
 __device__ __forceinline__ void add_counter(unsigned long long* c, uint32_t v) {
@@ -210,6 +206,7 @@ k_join_f32(const JoinParams P) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t nq4 = P.dpad >> 2;
   float4* sA = smem_f4 + (size_t)w * CH * nq4;
+  PairStage ps{reinterpret_cast<unsigned long long*>(smem_f4 + (size_t)(blockDim.x >> 5) * CH * nq4) + (size_t)w * PSTAGE, 0};
   const float4* X = (const float4*)P.xs;
   uint32_t band_cnt = 0, amb_cnt = 0;
   for (;;) {
@@ -259,10 +256,11 @@ k_join_f32(const JoinParams P) {
             if (sd <= P.eps2) acc_m |= 1u << a;
           }
         }
-        emit_pairs(P, acc_m, a0, q);
+        stage_hits(ps, P, acc_m, a0, q);
       }
     }
   }
+  stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
   add_counter(&P.ctr->band, band_cnt);
   add_counter(&P.ctr->ambiguous, amb_cnt);
 }
@@ -278,6 +276,7 @@ k_join_f32r(const JoinParams P) {
   extern __shared__ float4 smem_f4r[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   float4* sA = smem_f4r + (size_t)w * CH * DQ;
+  PairStage ps{reinterpret_cast<unsigned long long*>(smem_f4r + (size_t)(blockDim.x >> 5) * CH * DQ) + (size_t)w * PSTAGE, 0};
   const float4* X = (const float4*)P.xs;
   uint32_t band_cnt = 0, amb_cnt = 0;
   for (;;) {
@@ -341,10 +340,11 @@ k_join_f32r(const JoinParams P) {
             if (sd <= P.eps2) acc_m |= 1u << a;
           }
         }
-        emit_pairs(P, acc_m, a0, q);
+        stage_hits(ps, P, acc_m, a0, q);
       }
     }
   }
+  stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
   add_counter(&P.ctr->band, band_cnt);
   add_counter(&P.ctr->ambiguous, amb_cnt);
 }
@@ -388,6 +388,7 @@ k_join_f64(const JoinParams P) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t nq2 = P.dpad >> 1;
   double2* sA = smem_d2 + (size_t)w * CH * nq2;
+  PairStage ps{reinterpret_cast<unsigned long long*>(smem_d2 + (size_t)(blockDim.x >> 5) * CH * nq2) + (size_t)w * PSTAGE, 0};
   const double2* X = (const double2*)P.xs;
   const double thr = P.eps2 + P.amb;
   uint32_t amb_cnt = 0;
@@ -427,10 +428,11 @@ k_join_f64(const JoinParams P) {
         }
         acc_m &= m;
         amb_cnt += __popc(amb_m & m);
-        emit_pairs(P, acc_m, a0, q);
+        stage_hits(ps, P, acc_m, a0, q);
       }
     }
   }
+  stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
   add_counter(&P.ctr->ambiguous, amb_cnt);
 }
 
@@ -450,17 +452,22 @@ template <class K>
 static void launch_persistent(mistic_handle_s* h, K kern, size_t smem_per_warp, const JoinParams& P,
                               const char* name) {
   constexpr size_t kBlockSmem = 200 * 1024;
+  smem_per_warp += PSTAGE * sizeof(unsigned long long);  // pair staging buffer
   int warps = (int)std::min<size_t>(JOIN_THREADS / 32, std::max<size_t>(1, kBlockSmem / smem_per_warp));
   const size_t smem = smem_per_warp * warps;
   if (smem > kBlockSmem + 27 * 1024)
     throw Error(MISTIC_ERR_TOO_LARGE, "join tile does not fit in shared memory for this dimensionality");
   if (smem > 48 * 1024) MCK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  MCK(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
   MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));
   if (per_sm < 1) throw Error(MISTIC_ERR_TOO_LARGE, "join kernel does not fit on an SM for this dimensionality");
   const unsigned long long want = (P.n_units + warps - 1) / warps;
   const unsigned grid =
       (unsigned)std::min<unsigned long long>((unsigned long long)per_sm * h->sms, want ? want : 1);
+  if (getenv("MISTIC_DEBUG"))
+    fprintf(stderr, "[mistic] %s warps=%d smem=%zu occupancy=%d grid=%u units=%llu\n", name, warps, smem, per_sm, grid,
+            (unsigned long long)P.n_units);
   kern<<<grid, warps * 32, smem, h->stream>>>(P);
   launched(h, name);
 }

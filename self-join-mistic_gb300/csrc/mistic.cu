@@ -371,7 +371,10 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   }
   // tensor cores for large home bins when the FP32 view is usable and the
   // augmented K fits one operand tile
-  const bool use_tc = !fp64 && o.mode == MISTIC_MODE_BF16 && join::tc_supported(d) && eps2 > 1e-20;
+  // AUTO takes the tensor cores from d = 8 up (measured faster than the FP32
+  // filter on the 5M x 18 join); below that the augmented K is mostly padding
+  const bool use_tc = !fp64 && join::tc_supported(d) && eps2 > 1e-20 &&
+                      (o.mode == MISTIC_MODE_BF16 || (o.mode == MISTIC_MODE_AUTO && d >= 8));
   r->mode_used = fp64 ? MISTIC_MODE_FP64 : (use_tc ? MISTIC_MODE_BF16 : MISTIC_MODE_FP32);
   clk.mark();  // 5
 
@@ -438,12 +441,15 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     if ((double)tp.eps2_lo > eps2 / (1.0 + g64)) tp.eps2_lo = nextafterf(tp.eps2_lo, 0.f);
     tp.eps2_hi = (float)(eps2 / (1.0 - g64));
     if ((double)tp.eps2_hi < eps2 / (1.0 - g64)) tp.eps2_hi = nextafterf(tp.eps2_hi, INFINITY);
-    tp.kappa = (float)((3.02 * ldexp(1.0, -18) + n_mma * ldexp(1.0, -19) + gd) * (1.0 + gd) * 1.01);
+    // split error + MMA accumulation (2^-19 per instruction) + FP32 norms +
+    // rounding of the folded column |q'|^2 - T, per (|a'| + |q'|)^2 + 1.2 eps2
+    tp.kappa = (float)(((3.02 * ldexp(1.0, -18) + n_mma * 1.01 * ldexp(1.0, -19)) * (1.0 + gd) + gd + u) * 1.01);
     tp.ginf = (float)(1.0 / (1.0 - gd) * (1.0 + 1e-6));
     tp.uR2 = (float)(2.0 * u * R * 1.0001);
     tp.u1 = (float)(u * (1.0 + u) * 1.0001);
     tp.Dp = (float)(1.1 * sqrt(eps2));
     tp.cap = (float)(0.1 * eps2);
+    tp.margin = (float)(1e-6 * eps2);
   }
   const bool want_pairs = o.pairs != MISTIC_PAIRS_NONE;
   unsigned long long cap = 0;
@@ -481,6 +487,12 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   r->pairs_ordered_incl_self = 2 * hc.pairs + n;
   r->band_pairs = fp64 ? 0 : hc.band;
   r->ulp_ambiguous = hc.ambiguous;
+  if (use_tc) {
+    JoinCounters tcc{};
+    d2h(h, &tcc, ctr + 1, sizeof tcc);
+    r->tc_tiles = tcc.tiles;
+    r->tc_cells = tcc.cells;
+  }
 
   // ---- pair list
   mistic_status tail = MISTIC_OK;

@@ -43,6 +43,8 @@ class JoinResult:
     n_bin_pairs: int
     n_units: int
     n_units_tc: int
+    tc_tiles: int
+    tc_cells: int
     mode_used: str
     ms: dict
     kernel_launches: int
@@ -133,6 +135,7 @@ class Handle:
             pairs_ordered_incl_self=r.pairs_ordered_incl_self, candidates=r.candidates,
             band_pairs=r.band_pairs, ulp_ambiguous=r.ulp_ambiguous, n_bins=r.n_bins,
             n_bin_pairs=r.n_bin_pairs, n_units=r.n_units, n_units_tc=r.n_units_tc,
+            tc_tiles=r.tc_tiles, tc_cells=r.tc_cells,
             mode_used={0: "auto", 1: "fp64", 2: "fp32", 3: "bf16"}.get(r.mode_used, "?"),
             ms=ms, kernel_launches=r.kernel_launches, pairs=pairs, device_pairs=dev)
         if not keep_device or not r.pairs_on_device:

@@ -67,6 +67,8 @@ class Result(ctypes.Structure):
         ("n_bin_pairs", u64),
         ("n_units", u64),
         ("n_units_tc", u64),
+        ("tc_tiles", u64),
+        ("tc_cells", u64),
         ("pairs", ctypes.POINTER(u32)),
         ("pairs_len", u64),
         ("pairs_on_device", i32),

@@ -93,8 +93,10 @@ def test_modes_agree_and_band_is_small(handle):
     eps = 0.03
     a = run(handle, x, 6, eps, mode="fp32")
     b = run(handle, x, 6, eps, mode="fp64")
-    assert np.array_equal(a.pairs, b.pairs)
-    assert a.mode_used == "fp32" and b.mode_used == "fp64"
+    c = run(handle, x, 6, eps, mode="bf16")
+    assert np.array_equal(a.pairs, b.pairs) and np.array_equal(c.pairs, b.pairs)
+    assert a.mode_used == "fp32" and b.mode_used == "fp64" and c.mode_used == "bf16"
+    assert run(handle, x, 6, eps).mode_used == "bf16"  # AUTO at d = 18
     assert a.band_pairs < 0.01 * a.candidates + 1000
 
 
