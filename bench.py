@@ -66,12 +66,15 @@ def _subset(make, full_n):
 
 W.susy18.__wrapped_gen__ = lambda n: (W.gen_susy_like(n), 6, 64.0)
 W.uniform18.__wrapped_gen__ = lambda n: (W.gen_uniform(n, 18, seed=0), 6, 32.0)
+W.msd90.__wrapped_gen__ = lambda n: (W.gen_msd_like(n), 8, 16.0)
 
 WORKLOADS = {
     "susy18": (_subset(W.susy18, 5_000_000),
                "SUSY-shaped n=5e6 d=18 FP64, k=6, 64 mean neighbours"),
     "uniform18": (_subset(W.uniform18, 100_000),
                   "uniform n=1e5 d=18 FP64, k=6, 32 mean neighbours"),
+    "msd90": (_subset(W.msd90, 515_345),
+              "MSD-shaped n=515,345 d=90 FP64, k=8, 16 mean neighbours"),
 }
 
 FALLBACK_PEAKS = {"hbm_gbs": 6785.9, "bf16_tflops": 1922.1, "bf16_tflops_sustained": 1711.2}
@@ -299,10 +302,29 @@ def run_mistic(args, wl) -> None:
         return
     peaks = load_peaks()
     fp32_peak = measure_fp32_peak()
-    # dominant kernel: the FP32 filter join; algorithmic work 3d flops per
-    # candidate pair (d subtractions, d multiply-adds), CUDA-core FP32 pipe.
-    flops = r.candidates * 3.0 * d
-    achieved = flops / (join_ms * 1e-3) / 1e12
+    simt_ms = statistics.mean(q.ms["join_simt"] for q in results)
+    tc_ms = statistics.mean(q.ms["join_tc"] for q in results)
+    if r.mode_used == "bf16" and tc_ms >= simt_ms:
+        # dominant kernel: the tensor-core join; algorithmic work 2*d flops per
+        # evaluated (home row, candidate) cell, one contraction of length d
+        work = r.tc_cells * 2.0 * d
+        achieved = work / (tc_ms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "kernel": "k_join_tc", "achieved": achieved,
+                "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+                "frac": achieved / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
+                "traffic": None, "work": "2*d flops per evaluated cell (one d-long contraction)",
+                "peak_source": peaks["_source"] + " bf16 burst (of measured)", "kernel_ms": tc_ms,
+                "cells": r.tc_cells, "fp32_simt_peak_tflops": fp32_peak}
+    else:
+        # dominant kernel: the FP32 filter join; 3*d flops per candidate pair
+        # (d subtractions, d multiply-adds) on the CUDA-core FP32 pipe
+        work = r.candidates * 3.0 * d
+        achieved = work / (simt_ms * 1e-3) / 1e12
+        roof = {"bound": "fp32", "kernel": "k_join_f32r", "achieved": achieved, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                "work": "3*d FP32 flops per candidate pair", "kernel_ms": simt_ms,
+                "peak_source": "mistic_peaks FFMA probe, this run (CUDA-core FP32 pipe)"}
+    roof["hbm_peak_gbs"] = peaks.get("hbm_gbs")
     cpu = cpu_sample(x, wl.eps, args.cpu_seconds) if not args.no_cpu else None
     value = world * n / (ms * 1e-3)
     line = {
@@ -323,11 +345,7 @@ def run_mistic(args, wl) -> None:
         "tc_tiles": r.tc_tiles, "tc_fill": r.tc_cells / max(1, r.tc_tiles * 128 * 128),
         "k_used": r.k_used,
         "fp64_plain": fp64,
-        "roofline": {"bound": "fp32", "kernel": "k_join_f32", "achieved": achieved,
-                     "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None,
-                     "traffic": None, "work": "3*d FP32 flops per candidate pair",
-                     "peak_source": "mistic_peaks FFMA probe, this run (CUDA-core FP32 pipe)",
-                     "hbm_peak_gbs": peaks.get("hbm_gbs"), "hbm_peak_source": peaks["_source"]},
+        "roofline": roof,
         "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": n * d * x.itemsize, "d2h_bytes_per_step": int(r.pairs_ij) * 8,
                 "h2d_ms": statistics.mean(t[1] for t in e2e_res), "d2h_ms": statistics.mean(t[2] for t in e2e_res)},

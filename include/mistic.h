@@ -105,6 +105,9 @@ typedef struct mistic_opts {
                                  library allocates and the result owns the list */
   int32_t check_finite;       /* 1 (default): reject NaN/inf inputs with MISTIC_ERR_NOT_FINITE */
   int32_t timing;             /* 1 (default): fill the per-phase times */
+  mistic_pairs_where csr;     /* per-point neighbour table (CSR), the reference's neighborTable
+                                 (include/utils.cuh:33-41, built in src/launcher.cu:4-50):
+                                 NONE (default), HOST or DEVICE; see mistic_result.csr_* */
 } mistic_opts;
 
 typedef struct mistic_result {
@@ -127,8 +130,15 @@ typedef struct mistic_result {
   mistic_mode mode_used;
   /* per-phase device times (CUDA events on the handle's stream), ms */
   double ms_total, ms_h2d, ms_prep, ms_keys, ms_sort, ms_bins, ms_enum, ms_join, ms_d2h;
+  double ms_join_simt, ms_join_tc;  /* the two join kernels of the last join pass, ms */
   double ms_wall;                   /* host wall time of the whole call */
   uint32_t kernel_launches;         /* library kernels launched by this call */
+  /* CSR neighbour table when opts.csr != NONE: the neighbours of row i are
+   * csr_nbrs[csr_offsets[i] .. csr_offsets[i+1]), ascending, including i itself
+   * as the reference's table does; csr_offsets[n] == pairs_ordered_incl_self. */
+  uint64_t* csr_offsets;            /* n + 1 entries */
+  uint32_t* csr_nbrs;               /* csr_offsets[n] entries */
+  int32_t csr_on_device;
   void* _owner;                     /* internal: non-NULL when the result owns `pairs` */
 } mistic_result;
 

@@ -134,6 +134,8 @@ struct TcParams {
   float Dp;                // 1.1 sqrt(eps2)
   float cap;               // 0.1 eps2: larger bounds re-decide the whole column in FP64
   float margin;            // small positive slack that makes D' >= 0 a strict reject
+  long long wait_limit;    // try_wait iterations before a barrier wait gives up
+  int stall_test;          // failure-detection test: the MMA warp never signals (waits run out)
 };
 
 struct Timer {
@@ -153,6 +155,7 @@ struct mistic_handle_s {
   void* pinned = nullptr;  // small pinned block for scalar read-backs
   size_t pinned_bytes = 0;
   cudaEvent_t ev[16] = {};
+  cudaEvent_t jev[4] = {};  // around the two join kernels
   uint32_t launches = 0;
 };
 

@@ -191,9 +191,10 @@ __device__ __forceinline__ void prod_sync() { asm volatile("bar.sync 1, 128;" ::
 
 // Bounded wait; on expiry raise the CTA's abort flag.  Returns false if the
 // CTA is aborting (now or already).
-__device__ __forceinline__ bool wait_or_abort(unsigned long long* b, uint32_t parity, volatile uint32_t* abort_flag) {
+__device__ __forceinline__ bool wait_or_abort(unsigned long long* b, uint32_t parity, volatile uint32_t* abort_flag,
+                                              long long limit = kWaitLimit) {
   const uint32_t a = smem_u32(b);
-  for (long long it = 0; it < kWaitLimit; ++it) {
+  for (long long it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
                  : "=r"(done)
@@ -356,7 +357,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
     auto end_marker = [&]() {  // last tile slot: tells the MMA warp and the epilogue to stop
       const uint32_t st = tile % NS;
       if (tid == 0) {
-        wait_or_abort(&S.sfree[st], ((tile / NS) & 1) ^ 1, abort_flag);
+        wait_or_abort(&S.sfree[st], ((tile / NS) & 1) ^ 1, abort_flag, T.wait_limit);
         S.meta[st].flags = FLAG_END;
       }
       prod_sync();
@@ -367,7 +368,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
         const unsigned long long uu = atomicAdd(&T.ctr->next_unit, 1ull);
         S.unit = uu;
         bool go = uu < T.n_units && !*abort_flag;
-        if (go && unit_k > 0) go = wait_or_abort(&S.afree, (unit_k - 1) & 1, abort_flag);  // A no longer read
+        if (go && unit_k > 0) go = wait_or_abort(&S.afree, (unit_k - 1) & 1, abort_flag, T.wait_limit);  // A no longer read
         S.pflag = go ? 1u : 0u;
       }
       prod_sync();
@@ -452,7 +453,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
           continue;
         }
         const uint32_t st = tile % NS;
-        if (tid == 0) S.pflag = wait_or_abort(&S.sfree[st], ((tile / NS) & 1) ^ 1, abort_flag) ? 1u : 0u;
+        if (tid == 0) S.pflag = wait_or_abort(&S.sfree[st], ((tile / NS) & 1) ^ 1, abort_flag, T.wait_limit) ? 1u : 0u;
         prod_sync();
         if (!S.pflag) {
           aborted = true;
@@ -524,7 +525,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
       const uint32_t ah = smem_u32(Ahi), al = smem_u32(Alo);
       for (;;) {
         const uint32_t st = tile % NS, b = tile & 1;
-        if (!wait_or_abort(&S.full[st], (tile / NS) & 1, abort_flag)) {
+        if (!wait_or_abort(&S.full[st], (tile / NS) & 1, abort_flag, T.wait_limit)) {
           mbar_arrive(&S.dfull[b]);
           break;
         }
@@ -534,11 +535,15 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
           break;
         }
         bool ok = true;
-        if (flags & FLAG_FIRST) ok = wait_or_abort(&S.afull, unit_k & 1, abort_flag);
-        if (ok) ok = wait_or_abort(&S.dfree[b], ((tile >> 1) & 1) ^ 1, abort_flag);
+        if (flags & FLAG_FIRST) ok = wait_or_abort(&S.afull, unit_k & 1, abort_flag, T.wait_limit);
+        if (ok) ok = wait_or_abort(&S.dfree[b], ((tile >> 1) & 1) ^ 1, abort_flag, T.wait_limit);
         if (!ok) {
           mbar_arrive(&S.dfull[b]);
           break;
+        }
+        if (T.stall_test) {  // failure-detection test: never signal, let the waits run out
+          ++tile;
+          continue;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t bh = smem_u32(Bhi + st * OPB), bl = smem_u32(Blo + st * OPB);
@@ -563,7 +568,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
       // last committed tile, MMAs complete in issue order
       if (*abort_flag && last_b >= 0) {
         volatile uint32_t no_abort = 0;
-        wait_or_abort(&S.dfull[last_b], last_par, &no_abort);
+        wait_or_abort(&S.dfull[last_b], last_par, &no_abort, T.wait_limit);
       }
     }
     __syncwarp();
@@ -577,7 +582,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
     for (;;) {
       const uint32_t st = tile % NS, b = tile & 1;
       // all lanes wait; the outcome is made warp-uniform (tcgen05.ld is .sync.aligned)
-      const bool ok = __all_sync(FULL_MASK, wait_or_abort(&S.dfull[b], (tile >> 1) & 1, abort_flag));
+      const bool ok = __all_sync(FULL_MASK, wait_or_abort(&S.dfull[b], (tile >> 1) & 1, abort_flag, T.wait_limit));
       if (!ok) break;
       const TileMeta M = S.meta[st];
       if (__any_sync(FULL_MASK, (M.flags & FLAG_END) || *abort_flag)) break;

@@ -30,6 +30,9 @@
 namespace mistic {
 
 void pairs_to_ij(mistic_handle_s* h, unsigned long long* p, size_t n);
+void csr_edges(mistic_handle_s* h, const unsigned long long* pairs, size_t np, size_t n, unsigned long long* e);
+void csr_split(mistic_handle_s* h, const unsigned long long* e, size_t E, uint32_t* nbrs, unsigned long long* offs,
+               size_t n);
 
 // ------------------------------------------------------------------ plumbing
 
@@ -192,6 +195,8 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     throw Error(MISTIC_ERR_INVALID_ARG, "unknown mode");
   if (o.pairs != MISTIC_PAIRS_NONE && o.pairs != MISTIC_PAIRS_HOST && o.pairs != MISTIC_PAIRS_DEVICE)
     throw Error(MISTIC_ERR_INVALID_ARG, "unknown pairs destination");
+  if (o.csr != MISTIC_PAIRS_NONE && o.csr != MISTIC_PAIRS_HOST && o.csr != MISTIC_PAIRS_DEVICE)
+    throw Error(MISTIC_ERR_INVALID_ARG, "unknown csr destination");
   if (o.input_on_device && n > 0) {
     cudaPointerAttributes pa;
     MCK(cudaPointerGetAttributes(&pa, pts));
@@ -204,6 +209,23 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   r->mode_used = o.mode;
   if (n <= 1) {
     r->pairs_ordered_incl_self = n;
+    if (o.csr != MISTIC_PAIRS_NONE) {  // a lone point is its own neighbour
+      uint64_t off[2] = {0, n};
+      uint32_t nb[1] = {0};
+      if (o.csr == MISTIC_PAIRS_HOST) {
+        r->csr_offsets = (uint64_t*)malloc(sizeof off);
+        r->csr_nbrs = (uint32_t*)malloc(sizeof nb);
+        if (!r->csr_offsets || !r->csr_nbrs) throw Error(MISTIC_ERR_OUT_OF_MEMORY, "host csr");
+        memcpy(r->csr_offsets, off, (n + 1) * sizeof(uint64_t));
+        memcpy(r->csr_nbrs, nb, sizeof nb);
+      } else {
+        MCK(cudaMalloc((void**)&r->csr_offsets, sizeof off));
+        MCK(cudaMalloc((void**)&r->csr_nbrs, sizeof nb));
+        MCK(cudaMemcpy(r->csr_offsets, off, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice));
+        MCK(cudaMemcpy(r->csr_nbrs, nb, sizeof nb, cudaMemcpyHostToDevice));
+        r->csr_on_device = 1;
+      }
+    }
     r->ms_wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
     return;
   }
@@ -450,8 +472,16 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     tp.Dp = (float)(1.1 * sqrt(eps2));
     tp.cap = (float)(0.1 * eps2);
     tp.margin = (float)(1e-6 * eps2);
+    // MISTIC_TEST_TC_STALL=1 is the failure-detection test: the MMA warp
+    // signals nothing, every bounded wait runs out after a short limit, the
+    // kernel frees its tensor memory and the call returns MISTIC_ERR_TIMEOUT
+    const char* st = getenv("MISTIC_TEST_TC_STALL");
+    tp.stall_test = (st && *st == '1') ? 1 : 0;
+    tp.wait_limit = tp.stall_test ? (1ll << 12) : (1ll << 22);
   }
   const bool want_pairs = o.pairs != MISTIC_PAIRS_NONE;
+  const bool want_csr = o.csr != MISTIC_PAIRS_NONE;
+  const bool need_pairs = want_pairs || want_csr;  // the CSR table is built from the pair list
   unsigned long long cap = 0;
   unsigned long long* pbuf = nullptr;
   const bool caller_buf = want_pairs && o.pairs == MISTIC_PAIRS_DEVICE && o.pair_buffer;
@@ -460,7 +490,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     if ((uintptr_t)o.pair_buffer % 8) throw Error(MISTIC_ERR_INVALID_ARG, "pair_buffer must be 8-byte aligned");
     cap = o.pair_capacity;
     pbuf = (unsigned long long*)o.pair_buffer;
-  } else if (want_pairs) {
+  } else if (need_pairs) {
     cap = o.pair_capacity ? o.pair_capacity : std::max<unsigned long long>(1ull << 20, 16ull * n);
     auto it = h->arena.bufs.find("pairs");
     if (!o.pair_capacity && it != h->arena.bufs.end()) cap = std::max<unsigned long long>(cap, it->second.bytes / 8);
@@ -472,11 +502,14 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   JoinCounters hc{};
   for (int attempt = 0; attempt < 2; ++attempt) {
     MCK(cudaMemsetAsync(ctr, 0, 2 * sizeof(JoinCounters), h->stream));
+    if (o.timing) MCK(cudaEventRecord(h->jev[0], h->stream));
     join::run(h, fp64, CH, jp);
+    if (o.timing) MCK(cudaEventRecord(h->jev[1], h->stream));
     if (use_tc) join::run_tc(h, jp, tp);
+    if (o.timing) MCK(cudaEventRecord(h->jev[2], h->stream));
     d2h(h, &hc, ctr, sizeof hc);
     if (hc.error) throw Error(MISTIC_ERR_TIMEOUT, "a tensor-core tile wait timed out");
-    if (!want_pairs || hc.pairs <= cap || o.pair_capacity) break;
+    if (!need_pairs || hc.pairs <= cap || o.pair_capacity) break;
     cap = hc.pairs;
     pbuf = abuf<unsigned long long>(h, "pairs", cap);
     jp.pairs = pbuf;
@@ -494,8 +527,36 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     r->tc_cells = tcc.cells;
   }
 
-  // ---- pair list
+  // ---- CSR neighbour table (from the packed pair list, before it is sorted or converted)
   mistic_status tail = MISTIC_OK;
+  if (want_csr) {
+    const unsigned long long np = std::min<unsigned long long>(hc.pairs, cap);
+    if (hc.pairs > cap) tail = MISTIC_ERR_PAIR_OVERFLOW;
+    const unsigned long long E = 2 * np + n;
+    if (E >= 0xffffffffull) throw Error(MISTIC_ERR_TOO_LARGE, "neighbour table beyond 2^32 entries");
+    uint64_t* ek[2] = {abuf<uint64_t>(h, "csr_e0", E), abuf<uint64_t>(h, "csr_e1", E)};
+    csr_edges(h, pbuf, np, n, (unsigned long long*)ek[0]);
+    uint32_t* ev[2] = {nullptr, nullptr};
+    const int c = radix_sort_u64(h, ek, ev, false, false, E, 32 + std::max(1, bit_length(n - 1)));
+    uint64_t* offs = abuf<uint64_t>(h, "csr_off", n + 1);
+    uint32_t* nbs = abuf<uint32_t>(h, "csr_nbr", E);
+    csr_split(h, (const unsigned long long*)ek[c], E, nbs, (unsigned long long*)offs, n);
+    if (o.csr == MISTIC_PAIRS_HOST) {
+      r->csr_offsets = (uint64_t*)malloc((n + 1) * sizeof(uint64_t));
+      r->csr_nbrs = (uint32_t*)malloc(std::max<size_t>(1, E * sizeof(uint32_t)));
+      if (!r->csr_offsets || !r->csr_nbrs) throw Error(MISTIC_ERR_OUT_OF_MEMORY, "host csr table");
+      MCK(cudaMemcpyAsync(r->csr_offsets, offs, (n + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, h->stream));
+      MCK(cudaMemcpyAsync(r->csr_nbrs, nbs, E * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+      MCK(cudaStreamSynchronize(h->stream));
+    } else {
+      h->arena.bufs.erase("csr_off");  // the result owns them now
+      h->arena.bufs.erase("csr_nbr");
+      r->csr_offsets = offs;
+      r->csr_nbrs = nbs;
+      r->csr_on_device = 1;
+    }
+  }
+  // ---- pair list
   if (want_pairs) {
     const unsigned long long stored = std::min<unsigned long long>(hc.pairs, cap);
     if (hc.pairs > cap) tail = MISTIC_ERR_PAIR_OVERFLOW;
@@ -539,12 +600,59 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   r->ms_join = clk.ms(6, 7);
   r->ms_d2h = clk.ms(7, 8);
   r->ms_total = clk.ms(0, 8);
+  if (o.timing) {
+    float a = 0, b = 0;
+    MCK(cudaEventElapsedTime(&a, h->jev[0], h->jev[1]));
+    MCK(cudaEventElapsedTime(&b, h->jev[1], h->jev[2]));
+    r->ms_join_simt = a;
+    r->ms_join_tc = b;
+  }
   r->kernel_launches = h->launches - launches0;
   r->ms_wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
   if (tail != MISTIC_OK) throw Error(tail, "pair buffer smaller than the pair count; counts are valid");
 }
 
 }  // namespace
+
+// Directed edges of the neighbour table: both orientations of every pair
+// plus every point's self edge, packed (src << 32 | dst).
+__global__ void k_csr_edges(const unsigned long long* __restrict__ pairs, size_t np, size_t n,
+                            unsigned long long* __restrict__ e) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < np) {
+    const unsigned long long v = pairs[t];
+    e[2 * t] = v;
+    e[2 * t + 1] = (v << 32) | (v >> 32);
+  } else if (t < np + n) {
+    const unsigned long long p = t - np;
+    e[2 * np + p] = (p << 32) | p;
+  }
+}
+
+// Sorted edges -> neighbour ids and row offsets (every row has its self edge,
+// so every row starts somewhere).
+__global__ void k_csr_split(const unsigned long long* __restrict__ e, size_t E, uint32_t* __restrict__ nbrs,
+                            unsigned long long* __restrict__ offs, size_t n) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= E) return;
+  const unsigned long long v = e[t];
+  nbrs[t] = (uint32_t)v;
+  const unsigned long long src = v >> 32;
+  if (t == 0 || (e[t - 1] >> 32) != src) offs[src] = t;
+  if (t == 0) offs[n] = E;
+}
+
+void csr_edges(mistic_handle_s* h, const unsigned long long* pairs, size_t np, size_t n, unsigned long long* e) {
+  const size_t tot = np + n;
+  k_csr_edges<<<(unsigned)((tot + 255) / 256), 256, 0, h->stream>>>(pairs, np, n, e);
+  launched(h, "csr_edges");
+}
+
+void csr_split(mistic_handle_s* h, const unsigned long long* e, size_t E, uint32_t* nbrs, unsigned long long* offs,
+               size_t n) {
+  k_csr_split<<<(unsigned)((E + 255) / 256), 256, 0, h->stream>>>(e, E, nbrs, offs, n);
+  launched(h, "csr_split");
+}
 
 __global__ void k_pairs_to_ij(unsigned long long* p, size_t n) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -626,6 +734,7 @@ mistic_status mistic_create(mistic_handle* out, int device, void* stream) {
     }
     h->arena.stream = h->stream;
     for (auto& e : h->ev) MCK(cudaEventCreate(&e));
+    for (auto& e : h->jev) MCK(cudaEventCreate(&e));
   } catch (const Error& e) {
     mistic_status s = e.status;
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -643,6 +752,8 @@ mistic_status mistic_destroy(mistic_handle h) {
   h->arena.release_all();
   if (h->pinned) cudaFreeHost(h->pinned);
   for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : h->jev)
     if (e) cudaEventDestroy(e);
   if (h->own_stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -702,6 +813,15 @@ void mistic_result_free(mistic_result* r) {
   }
   r->pairs = nullptr;
   r->_owner = nullptr;
+  if (r->csr_on_device) {
+    if (r->csr_offsets) cudaFree(r->csr_offsets);
+    if (r->csr_nbrs) cudaFree(r->csr_nbrs);
+  } else {
+    free(r->csr_offsets);
+    free(r->csr_nbrs);
+  }
+  r->csr_offsets = nullptr;
+  r->csr_nbrs = nullptr;
   r->pairs_len = 0;
 }
 

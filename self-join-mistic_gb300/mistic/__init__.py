@@ -49,6 +49,8 @@ class JoinResult:
     ms: dict
     kernel_launches: int
     pairs: np.ndarray | None = None          # (P, 2) uint32 host array
+    csr_offsets: np.ndarray | None = None    # (n + 1,) uint64, host CSR table
+    csr_nbrs: np.ndarray | None = None       # (offsets[n],) uint32
     device_pairs: int | None = None          # device pointer when pairs="device"
     extra: dict = field(default_factory=dict)
 
@@ -89,7 +91,7 @@ class Handle:
 
     def opts(self, mode="auto", rp="pca", seed=0, pairs="none", sort_pairs=False,
              pair_capacity=0, input_on_device=False, check_finite=True, timing=True,
-             rp_user=None, pair_buffer=None) -> L.Opts:
+             rp_user=None, pair_buffer=None, csr="none") -> L.Opts:
         o = L.Opts()
         self.lib.mistic_opts_init(ctypes.byref(o))
         o.mode = MODES[mode]
@@ -103,6 +105,7 @@ class Handle:
         o.input_on_device = 1 if input_on_device else 0
         o.check_finite = 1 if check_finite else 0
         o.timing = 1 if timing else 0
+        o.csr = {"none": L.PAIRS_NONE, "host": L.PAIRS_HOST, "device": L.PAIRS_DEVICE}[csr]
         if rp_user is not None:
             self._rp_keep = np.ascontiguousarray(rp_user, dtype=np.float64)
             o.rp_user = self._rp_keep.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
@@ -128,8 +131,16 @@ class Handle:
                      if cnt else np.zeros((0, 2), np.uint32))
         elif r.pairs and r.pairs_on_device:
             dev = ctypes.cast(r.pairs, ctypes.c_void_p).value
+        csr_off = csr_nb = None
+        if r.csr_offsets and not r.csr_on_device:
+            n1 = int(r.n) + 1
+            csr_off = np.ctypeslib.as_array(r.csr_offsets, shape=(n1,)).copy()
+            tot = int(csr_off[-1])
+            csr_nb = (np.ctypeslib.as_array(r.csr_nbrs, shape=(tot,)).copy() if tot
+                      else np.zeros((0,), np.uint32))
         ms = {k: getattr(r, "ms_" + k) for k in
-              ("total", "h2d", "prep", "keys", "sort", "bins", "enum", "join", "d2h", "wall")}
+              ("total", "h2d", "prep", "keys", "sort", "bins", "enum", "join", "d2h", "join_simt",
+               "join_tc", "wall")}
         out = JoinResult(
             n=r.n, d=r.d, k_used=r.k_used, pairs_ij=r.pairs_ij,
             pairs_ordered_incl_self=r.pairs_ordered_incl_self, candidates=r.candidates,
@@ -137,7 +148,8 @@ class Handle:
             n_bin_pairs=r.n_bin_pairs, n_units=r.n_units, n_units_tc=r.n_units_tc,
             tc_tiles=r.tc_tiles, tc_cells=r.tc_cells,
             mode_used={0: "auto", 1: "fp64", 2: "fp32", 3: "bf16"}.get(r.mode_used, "?"),
-            ms=ms, kernel_launches=r.kernel_launches, pairs=pairs, device_pairs=dev)
+            ms=ms, kernel_launches=r.kernel_launches, pairs=pairs, device_pairs=dev,
+            csr_offsets=csr_off, csr_nbrs=csr_nb)
         if not keep_device or not r.pairs_on_device:
             self.lib.mistic_result_free(ctypes.byref(r))
         else:

@@ -51,6 +51,7 @@ class Opts(ctypes.Structure):
         ("pair_buffer", ctypes.POINTER(u32)),
         ("check_finite", i32),
         ("timing", i32),
+        ("csr", i32),
     ]
 
 
@@ -76,8 +77,12 @@ class Result(ctypes.Structure):
         ("ms_total", dbl), ("ms_h2d", dbl), ("ms_prep", dbl), ("ms_keys", dbl),
         ("ms_sort", dbl), ("ms_bins", dbl), ("ms_enum", dbl), ("ms_join", dbl),
         ("ms_d2h", dbl),
+        ("ms_join_simt", dbl), ("ms_join_tc", dbl),
         ("ms_wall", dbl),
         ("kernel_launches", u32),
+        ("csr_offsets", ctypes.POINTER(u64)),
+        ("csr_nbrs", ctypes.POINTER(u32)),
+        ("csr_on_device", i32),
         ("_owner", vp),
     ]
 

@@ -216,6 +216,7 @@ class Workload:
 EPS_HEX: dict[str, str] = {
     "uniform18:100000": "0x1.c37b06bdae65ep-1",
     "susy18:5000000": "0x1.55e138a251ac5p-7",
+    "msd90:515345": "0x1.c5a7e6636d473p+2",
 }
 
 

@@ -193,3 +193,48 @@ def test_device_input_and_device_pairs(handle):
     host = dev.cpu().numpy().view(np.uint32).reshape(-1, 2)
     handle.free_result(jr)
     assert np.array_equal(host, ref)
+
+
+def _csr_reference(ref_pairs, n):
+    """Neighbour table of the reference (include/utils.cuh:33-41): every row's
+    neighbours ascending, the row itself included."""
+    src = np.concatenate([ref_pairs[:, 0], ref_pairs[:, 1], np.arange(n, dtype=np.uint32)]).astype(np.int64)
+    dst = np.concatenate([ref_pairs[:, 1], ref_pairs[:, 0], np.arange(n, dtype=np.uint32)]).astype(np.int64)
+    order = np.lexsort((dst, src))
+    offs = np.zeros(n + 1, dtype=np.uint64)
+    offs[1:] = np.cumsum(np.bincount(src, minlength=n))
+    return offs, dst[order].astype(np.uint32)
+
+
+@pytest.mark.parametrize("mode", ["auto", "fp32", "fp64"])
+def test_csr_neighbour_table(handle, mode):
+    x = np.random.default_rng(31).random((6000, 7))
+    eps = 0.18
+    ref = O.brute_pairs(x, eps)
+    offs, nbrs = _csr_reference(ref, 6000)
+    r = handle.selfjoin(x, 5, eps, mode=mode, csr="host", pairs="host", sort_pairs=True)
+    assert np.array_equal(r.pairs, ref)
+    assert np.array_equal(r.csr_offsets, offs)
+    assert np.array_equal(r.csr_nbrs, nbrs)
+    assert int(r.csr_offsets[-1]) == r.pairs_ordered_incl_self
+
+
+def test_csr_device_and_edges(handle):
+    torch = pytest.importorskip("torch")
+    x = np.random.default_rng(32).normal(size=(4000, 12))
+    eps = 2.5
+    ref = O.brute_pairs(x, eps)
+    offs, nbrs = _csr_reference(ref, 4000)
+    o = handle.opts(csr="device")
+    raw = handle.selfjoin_raw(x.ctypes.data, 4000, 12, L.F64, 6, eps, o)
+    import ctypes
+    op = ctypes.cast(raw.csr_offsets, ctypes.c_void_p).value
+    npp = ctypes.cast(raw.csr_nbrs, ctypes.c_void_p).value
+    assert raw.csr_on_device == 1
+    d_off = torch.as_tensor(_DevView(op, 2 * 4001), device="cuda").cpu().numpy().view(np.uint64)
+    d_nbr = torch.as_tensor(_DevView(npp, len(nbrs)), device="cuda").cpu().numpy().view(np.uint32)
+    handle.lib.mistic_result_free(ctypes.byref(raw))
+    assert np.array_equal(d_off, offs) and np.array_equal(d_nbr, nbrs)
+    for n in (0, 1):
+        r = handle.selfjoin(np.zeros((n, 3)), 2, 1.0, csr="host")
+        assert r.csr_offsets.tolist() == list(range(n + 1)) and r.csr_nbrs.tolist() == list(range(n))
