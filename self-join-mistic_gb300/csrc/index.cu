@@ -96,40 +96,68 @@ __global__ void k_gather_sample(const T* __restrict__ x, size_t n, uint32_t d, u
   s[i] = ld(x, src * d + col);
 }
 
-// cov[a][b] = mean over the sample of (s_a - mu_a)(s_b - mu_b); mu = sample mean
-__global__ void k_sample_cov(const double* __restrict__ s, uint32_t S, uint32_t d,
-                             double* __restrict__ cov) {
-  const uint32_t a = blockIdx.y * blockDim.y + threadIdx.y;
-  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= d || b >= d || b < a) return;
-  double ma = 0, mb = 0;
-  for (uint32_t r = 0; r < S; ++r) {
-    ma += s[(size_t)r * d + a];
-    mb += s[(size_t)r * d + b];
+// Sample covariance about the full-data mean mu: each block accumulates a
+// 16 x 16 tile of (a, b) over one chunk of sample rows (staged in shared
+// memory); a second kernel adds the chunk partials in a fixed order, so the
+// result - and the reference points derived from it - is deterministic.
+constexpr int COV_T = 16;
+constexpr int COV_CHUNK = 128;
+
+__global__ void k_sample_cov_part(const double* __restrict__ s, uint32_t S, uint32_t d, const double* __restrict__ mu,
+                                  double* __restrict__ part /* [chunks][d][d] */) {
+  __shared__ double sa[COV_CHUNK][COV_T + 1], sb[COV_CHUNK][COV_T + 1];
+  const uint32_t a0 = blockIdx.y * COV_T, b0 = blockIdx.x * COV_T, r0 = blockIdx.z * COV_CHUNK;
+  const int tx = threadIdx.x, ty = threadIdx.y, t = ty * COV_T + tx;
+  for (int i = t; i < COV_CHUNK * COV_T; i += COV_T * COV_T) {
+    const int rr = i / COV_T, cc = i % COV_T;
+    const uint32_t row = r0 + rr;
+    double va = 0.0, vb = 0.0;
+    if (row < S && a0 + cc < d) va = s[(size_t)row * d + a0 + cc] - mu[a0 + cc];
+    if (row < S && b0 + cc < d) vb = s[(size_t)row * d + b0 + cc] - mu[b0 + cc];
+    sa[rr][cc] = va;
+    sb[rr][cc] = vb;
   }
-  ma /= S;
-  mb /= S;
-  double c = 0;
-  for (uint32_t r = 0; r < S; ++r) c += (s[(size_t)r * d + a] - ma) * (s[(size_t)r * d + b] - mb);
-  c /= S;
-  cov[(size_t)a * d + b] = c;
-  cov[(size_t)b * d + a] = c;
+  __syncthreads();
+  double acc = 0.0;
+  for (int rr = 0; rr < COV_CHUNK; ++rr) acc = fma(sa[rr][ty], sb[rr][tx], acc);
+  const uint32_t a = a0 + ty, b = b0 + tx;
+  if (a < d && b < d) part[((size_t)blockIdx.z * d + a) * d + b] = acc;
+}
+
+__global__ void k_sample_cov_final(const double* __restrict__ part, uint32_t chunks, uint32_t d, uint32_t S,
+                                   double* __restrict__ cov) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)d * d) return;
+  double acc = 0.0;
+  for (uint32_t c = 0; c < chunks; ++c) acc += part[(size_t)c * d * d + i];
+  cov[i] = acc / S;
 }
 
 // ------------------------------------------------------------ reference-point distances
 // D[i][j] = FP64 ||x_i - r_j|| (sequential sum, then sqrt), with per-block
 // min/max partials per reference point.
 constexpr int RPD_THREADS = 256;
+constexpr uint32_t RPD_DMAX = 48;  // rows staged in shared memory up to this d
 
 template <class T>
 __global__ void __launch_bounds__(RPD_THREADS)
 k_rp_dist(const T* __restrict__ x, size_t n, uint32_t d, const double* __restrict__ rps, int k,
           double* __restrict__ D, double* __restrict__ part /* [block][2][k] */) {
-  extern __shared__ double srp[];  // k x d
+  // dynamic shared memory: k x d reference points, then a tile of rows
+  // (RPD_THREADS rows of up to RPD_DMAX coordinates) copied with coalesced loads
+  extern __shared__ double srp[];
+  double* tile = srp + (size_t)k * d;
   for (uint32_t i = threadIdx.x; i < (uint32_t)k * d; i += blockDim.x) srp[i] = rps[i];
   __shared__ double smn[MAX_K][RPD_THREADS / 32], smx[MAX_K][RPD_THREADS / 32];
+  const size_t row0 = (size_t)blockIdx.x * blockDim.x;
+  const uint32_t rows = (uint32_t)min((size_t)blockDim.x, n > row0 ? n - row0 : 0);
+  const bool staged = d <= RPD_DMAX;
+  if (staged) {
+    const size_t base = row0 * d;
+    for (uint32_t i = threadIdx.x; i < rows * d; i += blockDim.x) tile[i] = (double)x[base + i];
+  }
   __syncthreads();
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t i = row0 + threadIdx.x;
   const bool valid = i < n;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int j = 0; j < k; ++j) {
@@ -138,7 +166,8 @@ k_rp_dist(const T* __restrict__ x, size_t n, uint32_t d, const double* __restric
       double s = 0.0;
       const double* r = srp + (size_t)j * d;
       for (uint32_t t = 0; t < d; ++t) {
-        double df = ld(x, i * d + t) - r[t];
+        const double xv = staged ? tile[(size_t)threadIdx.x * d + t] : (double)x[i * d + t];
+        const double df = xv - r[t];
         s = fma(df, df, s);
       }
       dist = sqrt(s);
@@ -170,15 +199,32 @@ k_rp_dist(const T* __restrict__ x, size_t n, uint32_t d, const double* __restric
 
 __global__ void k_minmax_final(const double* __restrict__ part, uint32_t nparts, int k,
                                double* __restrict__ out /* min[k], max[k] */) {
-  const int j = threadIdx.x;
-  if (j >= k) return;
+  // one block per reference point; fixed reduction order (deterministic)
+  const int j = blockIdx.x;
   double mn = INFINITY, mx = -INFINITY;
-  for (uint32_t b = 0; b < nparts; ++b) {
+  for (uint32_t b = threadIdx.x; b < nparts; b += blockDim.x) {
     mn = fmin(mn, part[(size_t)b * 2 * k + j]);
     mx = fmax(mx, part[(size_t)b * 2 * k + k + j]);
   }
-  out[j] = mn;
-  out[k + j] = mx;
+  __shared__ double smn[32], smx[32];
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    mn = fmin(mn, __shfl_xor_sync(FULL_MASK, mn, o));
+    mx = fmax(mx, __shfl_xor_sync(FULL_MASK, mx, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    smn[threadIdx.x >> 5] = mn;
+    smx[threadIdx.x >> 5] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      mn = fmin(mn, smn[w]);
+      mx = fmax(mx, smx[w]);
+    }
+    out[j] = mn;
+    out[k + j] = mx;
+  }
 }
 
 // ------------------------------------------------------------ key packing
@@ -428,7 +474,7 @@ void colstats(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, uint
 }
 
 void sample_cov(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, uint32_t d,
-                uint32_t S, double* sbuf, double* cov) {
+                uint32_t S, double* sbuf, const double* mu, double* part, double* cov) {
   const size_t tot = (size_t)S * d;
   const unsigned nb = (unsigned)((tot + 255) / 256);
   if (dt == MISTIC_F64)
@@ -436,14 +482,17 @@ void sample_cov(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, ui
   else
     k_gather_sample<float><<<nb, 256, 0, h->stream>>>((const float*)x, n, d, S, sbuf);
   launched(h, "gather_sample");
-  dim3 blk(16, 16), grd((d + 15) / 16, (d + 15) / 16);
-  k_sample_cov<<<grd, blk, 0, h->stream>>>(sbuf, S, d, cov);
-  launched(h, "sample_cov");
+  const uint32_t chunks = (S + COV_CHUNK - 1) / COV_CHUNK;
+  dim3 blk(COV_T, COV_T), grd((d + COV_T - 1) / COV_T, (d + COV_T - 1) / COV_T, chunks);
+  k_sample_cov_part<<<grd, blk, 0, h->stream>>>(sbuf, S, d, mu, part);
+  launched(h, "sample_cov_part");
+  k_sample_cov_final<<<(unsigned)(((size_t)d * d + 255) / 256), 256, 0, h->stream>>>(part, chunks, d, S, cov);
+  launched(h, "sample_cov_final");
 }
 
 void rp_dist(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, uint32_t d,
              const double* rps, int k, double* D, double* part, uint32_t nparts, double* mm) {
-  const size_t smem = (size_t)k * d * sizeof(double);
+  const size_t smem = (size_t)k * d * sizeof(double) + (d <= RPD_DMAX ? (size_t)RPD_THREADS * d * sizeof(double) : 0);
   if (smem > 48 * 1024) {
     if (dt == MISTIC_F64)
       MCK(cudaFuncSetAttribute(k_rp_dist<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -455,7 +504,7 @@ void rp_dist(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, uint3
   else
     k_rp_dist<float><<<nparts, RPD_THREADS, smem, h->stream>>>((const float*)x, n, d, rps, k, D, part);
   launched(h, "rp_dist");
-  k_minmax_final<<<1, 32, 0, h->stream>>>(part, nparts, k, mm);
+  k_minmax_final<<<k, 256, 0, h->stream>>>(part, nparts, k, mm);
   launched(h, "minmax_final");
 }
 

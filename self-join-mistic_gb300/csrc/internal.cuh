@@ -181,7 +181,7 @@ namespace idx {
 void colstats(mistic_handle_s*, const void* x, mistic_dtype, size_t n, uint32_t d, double* part,
               uint32_t nparts, double* out, unsigned* nonfinite);
 void sample_cov(mistic_handle_s*, const void* x, mistic_dtype, size_t n, uint32_t d, uint32_t S,
-                double* sbuf, double* cov);
+                double* sbuf, const double* mu, double* part, double* cov);
 void rp_dist(mistic_handle_s*, const void* x, mistic_dtype, size_t n, uint32_t d, const double* rps,
              int k, double* D, double* part, uint32_t nparts, double* mm);
 void pack_keys(mistic_handle_s*, const double* D, size_t n, const PackParams&, uint64_t* keys);

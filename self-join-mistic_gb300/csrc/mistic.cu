@@ -255,7 +255,8 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   if (pca) {
     double* sbuf = abuf<double>(h, "sample", (size_t)S * d);
     cov = abuf<double>(h, "cov", (size_t)d * d);
-    idx::sample_cov(h, x, dt, n, d, S, sbuf, cov);
+    double* cpart = abuf<double>(h, "cov_part", (size_t)((S + 127) / 128) * d * d);
+    idx::sample_cov(h, x, dt, n, d, S, sbuf, cs_out /* full-data column means */, cpart, cov);
   }
   std::vector<double> stats(3 * (size_t)d);
   unsigned nonfinite = 0;
