@@ -77,6 +77,7 @@ struct JoinCounters {
   unsigned long long error;      // non-zero: a bounded device wait gave up
   unsigned long long tiles;      // tensor-core tiles evaluated
   unsigned long long cells;      // sum over those tiles of home rows x candidate columns
+  unsigned long long prof[8];    // role cycle breakdown when TcParams.prof is set
 };
 
 // Key packing: field f = floor((D[i*kstride + col[f]] - dmin[f]) / w[f]),
@@ -136,6 +137,7 @@ struct TcParams {
   float margin;            // small positive slack that makes D' >= 0 a strict reject
   long long wait_limit;    // try_wait iterations before a barrier wait gives up
   int stall_test;          // failure-detection test: the MMA warp never signals (waits run out)
+  int prof;                // record per-role wait/total cycles into ctr->prof (diagnostics)
 };
 
 struct Timer {
@@ -209,6 +211,7 @@ void run(mistic_handle_s*, bool fp64, int CH, const JoinParams&);
 // Tensor-core join over TcParams.units; KP = augmented K (d + 2 rounded up to 16).
 bool tc_supported(uint32_t d);
 int tc_kp(uint32_t d);
+uint32_t tc_rows(uint32_t d);
 void run_tc(mistic_handle_s*, const JoinParams&, const TcParams&);
 }  // namespace join
 

@@ -91,17 +91,6 @@ __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&v)[3
 }
 __device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-        "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-        "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;");
-}
 
 __device__ __forceinline__ double exact_sqdist_tc(const JoinParams& P, uint32_t i, uint32_t j) {
   double s = 0.0;
@@ -156,13 +145,16 @@ constexpr int NPROD = 128;
 constexpr uint32_t FLAG_FIRST = 1, FLAG_LAST = 2, FLAG_END = 4;
 
 struct TileMeta {
-  uint32_t a0, na, hs, he, ncols, flags;
+  uint32_t a0, na, hs, he, ncols, flags, ng;  // ng: 128-row MMA tiles of this unit (1..G)
 };
 
-template <int NS>
+template <int NS, int G>
 struct TcShared2 {
   __align__(16) float center[128];
   uint32_t qpos[NS][TN];
+  uint32_t qid[NS][TN];      // original row ids of the candidates
+  uint32_t aid[NS][TM * G];  // original row ids of the home rows (per stage: the epilogue
+                             // may still read a finished unit while producers start the next)
   float dlt[NS][TN];  // accept when D' <= -dlt
   TileMeta meta[NS];
   uint32_t w_start[WIN];
@@ -309,14 +301,14 @@ __device__ __forceinline__ bool column_threshold(const TcParams& T, float ra2max
   return true;
 }
 
-template <int KP, int NS>
+template <int KP, int NS, int G>
 __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, const TcParams T) {
   extern __shared__ __align__(128) unsigned char tc_dyn[];
-  __shared__ TcShared2<NS> S;
+  __shared__ TcShared2<NS, G> S;
   constexpr uint32_t OPB = TM * KP;  // bf16 elements per operand buffer
-  __nv_bfloat16* Ahi = reinterpret_cast<__nv_bfloat16*>(tc_dyn);
-  __nv_bfloat16* Alo = Ahi + OPB;
-  __nv_bfloat16* Bhi = Alo + OPB;  // NS stages of hi, then NS stages of lo
+  __nv_bfloat16* Ahi = reinterpret_cast<__nv_bfloat16*>(tc_dyn);  // G home chunks of 128 rows
+  __nv_bfloat16* Alo = Ahi + G * OPB;
+  __nv_bfloat16* Bhi = Alo + G * OPB;  // NS stages of hi, then NS stages of lo
   __nv_bfloat16* Blo = Bhi + NS * OPB;
   float* sv = reinterpret_cast<float*>(Blo + NS * OPB);  // 4 epilogue warps x 32 lanes x SV_STRIDE
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -354,6 +346,8 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
     // and broadcast through S.pflag.
     uint32_t tile = 0, unit_k = 0;
     unsigned long long n_tiles = 0, n_cells = 0;
+    long long pw_sfree = 0;
+    const long long p_start = T.prof ? clock64() : 0;
     auto end_marker = [&]() {  // last tile slot: tells the MMA warp and the epilogue to stop
       const uint32_t st = tile % NS;
       if (tid == 0) {
@@ -379,21 +373,28 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
       const unsigned long long u = S.unit;
       const Unit U = T.units[u];
       const uint32_t hs = P.bstart[U.h], he = P.bstart[U.h + 1];
-      const uint32_t a0 = hs + U.chunk * TM;
-      const uint32_t na = min((uint32_t)TM, he - a0);
+      const uint32_t a0 = hs + U.chunk * (TM * G);
+      const uint32_t na = min((uint32_t)(TM * G), he - a0);
+      const uint32_t ng = (na + TM - 1) / TM;
       if (tid < (int)P.dpad) S.center[tid] = X[(size_t)a0 * P.dpad + tid];
       if (tid == 0) S.ra2max = 0;
       prod_sync();
+      uint32_t my_aid[G];  // original ids of home rows tid, 128 + tid, ...
+#pragma unroll
+      for (int g = 0; g < G; ++g) my_aid[g] = (uint32_t)(g * TM + tid) < na ? P.ids[a0 + g * TM + tid] : 0u;
       {
-        float nrm = 0.f;
-        if ((uint32_t)tid < na) {
-          const float* xr = X + (size_t)(a0 + tid) * P.dpad;
-          nrm = row_norm(xr, S.center, P.d, P.dpad);
-          write_row2<KP>(Ahi, Alo, tid, xr, S.center, P.d, P.dpad, true, nrm, 0.f);
-        } else {
-          zero_row2<KP>(Ahi, Alo, tid);
+        float m = 0.f;
+        for (uint32_t g = 0; g < ng; ++g) {
+          const uint32_t r = g * TM + tid;
+          if (r < na) {
+            const float* xr = X + (size_t)(a0 + r) * P.dpad;
+            const float nrm = row_norm(xr, S.center, P.d, P.dpad);
+            write_row2<KP>(Ahi + g * OPB, Alo + g * OPB, tid, xr, S.center, P.d, P.dpad, true, nrm, 0.f);
+            m = fmaxf(m, nrm);
+          } else {
+            zero_row2<KP>(Ahi + g * OPB, Alo + g * OPB, tid);
+          }
         }
-        float m = nrm;
 #pragma unroll
         for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL_MASK, m, o));
         if (lane == 0) atomicMax(&S.ra2max, __float_as_uint(m));
@@ -453,7 +454,11 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
           continue;
         }
         const uint32_t st = tile % NS;
-        if (tid == 0) S.pflag = wait_or_abort(&S.sfree[st], ((tile / NS) & 1) ^ 1, abort_flag, T.wait_limit) ? 1u : 0u;
+        if (tid == 0) {
+          const long long c0 = T.prof ? clock64() : 0;
+          S.pflag = wait_or_abort(&S.sfree[st], ((tile / NS) & 1) ^ 1, abort_flag, T.wait_limit) ? 1u : 0u;
+          if (T.prof) pw_sfree += clock64() - c0;
+        }
         prod_sync();
         if (!S.pflag) {
           aborted = true;
@@ -474,6 +479,9 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
           q = S.w_start[lo] + (rank - S.w_pref[lo]);
         }
         S.qpos[st][tid] = q;
+        S.qid[st][tid] = (uint32_t)tid < ncols ? P.ids[q] : 0u;
+#pragma unroll
+        for (int g = 0; g < G; ++g) S.aid[st][g * TM + tid] = my_aid[g];
         __nv_bfloat16* bh = Bhi + st * OPB;
         __nv_bfloat16* bl = Blo + st * OPB;
         if ((uint32_t)tid < ncols) {
@@ -492,7 +500,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
           S.dlt[st][tid] = 0.f;
         }
         if (tid == 0) {
-          S.meta[st] = TileMeta{a0, na, hs, he, ncols, (first ? FLAG_FIRST : 0u) | (last ? FLAG_LAST : 0u)};
+          S.meta[st] = TileMeta{a0, na, hs, he, ncols, (first ? FLAG_FIRST : 0u) | (last ? FLAG_LAST : 0u), ng};
           n_tiles += 1;
           n_cells += (unsigned long long)na * ncols;
         }
@@ -514,55 +522,83 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
       atomicAdd(&T.ctr->tiles, n_tiles);
       atomicAdd(&T.ctr->cells, n_cells);
     }
+    if (tid == 0 && T.prof) {
+      atomicAdd(&T.ctr->prof[0], (unsigned long long)pw_sfree);
+      atomicAdd(&T.ctr->prof[1], (unsigned long long)(clock64() - p_start));
+    }
   } else if (warp == 8) {
     // ============================ MMA issuer
+    // B tiles come in stage order; each is multiplied with the unit's ng home
+    // chunks into alternating TMEM accumulators (MMA tile counter mt).
     if (lane == 0) {
       constexpr uint32_t idesc = umma_idesc(TM, TN);
       constexpr uint32_t SBO = 16u * KP;
-      uint32_t tile = 0, unit_k = 0;
+      uint32_t tile = 0, mt = 0, unit_k = 0;
       int last_b = -1;
       uint32_t last_par = 0;
-      const uint32_t ah = smem_u32(Ahi), al = smem_u32(Alo);
+      long long mw_full = 0, mw_dfree = 0;
+      const long long m_start = T.prof ? clock64() : 0;
       for (;;) {
-        const uint32_t st = tile % NS, b = tile & 1;
-        if (!wait_or_abort(&S.full[st], (tile / NS) & 1, abort_flag, T.wait_limit)) {
-          mbar_arrive(&S.dfull[b]);
+        const uint32_t st = tile % NS;
+        const long long c0 = T.prof ? clock64() : 0;
+        const bool fok = wait_or_abort(&S.full[st], (tile / NS) & 1, abort_flag, T.wait_limit);
+        if (T.prof) mw_full += clock64() - c0;
+        if (!fok) {
+          mbar_arrive(&S.dfull[mt & 1]);
           break;
         }
         const uint32_t flags = S.meta[st].flags;
+        const uint32_t ng = S.meta[st].ng;
         if (flags & FLAG_END) {
-          mbar_arrive(&S.dfull[b]);
+          mbar_arrive(&S.dfull[mt & 1]);
           break;
         }
         bool ok = true;
         if (flags & FLAG_FIRST) ok = wait_or_abort(&S.afull, unit_k & 1, abort_flag, T.wait_limit);
-        if (ok) ok = wait_or_abort(&S.dfree[b], ((tile >> 1) & 1) ^ 1, abort_flag, T.wait_limit);
         if (!ok) {
-          mbar_arrive(&S.dfull[b]);
+          mbar_arrive(&S.dfull[mt & 1]);
           break;
         }
-        if (T.stall_test) {  // failure-detection test: never signal, let the waits run out
-          ++tile;
-          continue;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t bh = smem_u32(Bhi + st * OPB), bl = smem_u32(Blo + st * OPB);
-        const uint32_t dt = tbase + b * TN;
+        for (uint32_t g = 0; g < ng && ok; ++g) {
+          const uint32_t b = mt & 1;
+          const long long c1 = T.prof ? clock64() : 0;
+          ok = wait_or_abort(&S.dfree[b], ((mt >> 1) & 1) ^ 1, abort_flag, T.wait_limit);
+          if (T.prof) mw_dfree += clock64() - c1;
+          if (!ok) {
+            mbar_arrive(&S.dfull[b]);
+            break;
+          }
+          if (T.stall_test) {  // failure-detection test: never signal, let the waits run out
+            ++mt;
+            continue;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t ah = smem_u32(Ahi + g * OPB), al = smem_u32(Alo + g * OPB);
+          const uint32_t dt = tbase + b * TN;
 #pragma unroll
-        for (int ks = 0; ks < KP / 16; ++ks) {
-          const uint32_t o = ks * 256;
-          mma_bf16(dt, umma_desc(ah + o, SBO), umma_desc(bh + o, SBO), idesc, ks > 0 ? 1u : 0u);
-          mma_bf16(dt, umma_desc(ah + o, SBO), umma_desc(bl + o, SBO), idesc, 1u);
-          mma_bf16(dt, umma_desc(al + o, SBO), umma_desc(bh + o, SBO), idesc, 1u);
+          for (int ks = 0; ks < KP / 16; ++ks) {
+            const uint32_t o = ks * 256;
+            mma_bf16(dt, umma_desc(ah + o, SBO), umma_desc(bh + o, SBO), idesc, ks > 0 ? 1u : 0u);
+            mma_bf16(dt, umma_desc(ah + o, SBO), umma_desc(bl + o, SBO), idesc, 1u);
+            mma_bf16(dt, umma_desc(al + o, SBO), umma_desc(bh + o, SBO), idesc, 1u);
+          }
+          tc_commit(&S.dfull[b]);
+          last_b = (int)b;
+          last_par = (mt >> 1) & 1;
+          ++mt;
         }
-        tc_commit(&S.dfull[b]);
-        last_b = (int)b;
-        last_par = (tile >> 1) & 1;
-        if (flags & FLAG_LAST) {
+        if (!ok) break;
+        if ((flags & FLAG_LAST) && !T.stall_test) {
           tc_commit(&S.afree);
           ++unit_k;
         }
         ++tile;
+      }
+      if (T.prof) {
+        atomicAdd(&T.ctr->prof[2], (unsigned long long)mw_full);
+        atomicAdd(&T.ctr->prof[3], (unsigned long long)mw_dfree);
+        atomicAdd(&T.ctr->prof[4], (unsigned long long)(clock64() - m_start));
       }
       // an aborting CTA may still have MMAs in flight: wait (bounded) for the
       // last committed tile, MMAs complete in issue order
@@ -578,16 +614,20 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
     float* my_sv = sv + (size_t)(quarter * 32 + lane) * SV_STRIDE;
     PairStage ps{reinterpret_cast<unsigned long long*>(sv + (size_t)4 * 32 * SV_STRIDE) + quarter * PSTAGE, 0};
     uint32_t band_cnt = 0, amb_cnt = 0;
-    uint32_t tile = 0;
+    uint32_t tile = 0, mt = 0, g = 0;
+    long long ew_dfull = 0;
+    const long long e_start = T.prof ? clock64() : 0;
     for (;;) {
-      const uint32_t st = tile % NS, b = tile & 1;
+      const uint32_t st = tile % NS, b = mt & 1;
       // all lanes wait; the outcome is made warp-uniform (tcgen05.ld is .sync.aligned)
-      const bool ok = __all_sync(FULL_MASK, wait_or_abort(&S.dfull[b], (tile >> 1) & 1, abort_flag, T.wait_limit));
+      const long long c0 = T.prof ? clock64() : 0;
+      const bool ok = __all_sync(FULL_MASK, wait_or_abort(&S.dfull[b], (mt >> 1) & 1, abort_flag, T.wait_limit));
+      if (T.prof) ew_dfull += clock64() - c0;
       if (!ok) break;
       const TileMeta M = S.meta[st];
       if (__any_sync(FULL_MASK, (M.flags & FLAG_END) || *abort_flag)) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t row = quarter * 32 + lane;
+      const uint32_t row = g * TM + quarter * 32 + lane;  // row within the unit
       const bool row_ok = row < M.na;
       const uint32_t a_sorted = M.a0 + row;
       // a quarter whose 32 rows all lie past the home chunk has nothing to do;
@@ -618,7 +658,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
               if (my_sv[j] <= -S.dlt[st][c0 + j]) {
                 acc_bits |= 1u << j;
               } else {
-                const double sd = exact_sqdist_tc(P, P.ids[a_sorted], P.ids[q]);
+                const double sd = exact_sqdist_tc(P, S.aid[st][row], S.qid[st][c0 + j]);
                 ++band_cnt;
                 if (fabs(sd - P.eps2) <= P.amb) ++amb_cnt;
                 if (sd <= P.eps2) acc_bits |= 1u << j;
@@ -627,21 +667,21 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
           }
         }
         {
-          const uint32_t ia = acc_bits ? P.ids[a_sorted] : 0u;
+          const uint32_t ia = acc_bits ? S.aid[st][row] : 0u;
           uint32_t bits = acc_bits;
           stage_pairs(
               ps, __popc(acc_bits),
               [&](uint32_t) {
                 const int j = __ffs(bits) - 1;
                 bits &= bits - 1;
-                const uint32_t iq = P.ids[S.qpos[st][c0 + j]];
+                const uint32_t iq = S.qid[st][c0 + j];
                 const uint32_t lo = ia < iq ? ia : iq, hi = ia < iq ? iq : ia;
                 return ((unsigned long long)lo << 32) | hi;
               },
               &P.ctr->pairs, P.pairs, P.cap);
         }
             };
-      if (quarter * 32 < M.na) {
+      if (g * TM + quarter * 32 < M.na) {
         for (uint32_t c0 = 0; c0 < M.ncols; c0 += 64) {
           uint32_t v0[32], v1[32];
           const uint32_t ta = tbase + b * TN + ((quarter * 32u) << 16) + c0;
@@ -654,13 +694,24 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
+      const bool last_g = g + 1 >= M.ng;
       if (lane == 0) {
         mbar_arrive(&S.dfree[b]);
-        mbar_arrive(&S.sfree[st]);
+        if (last_g) mbar_arrive(&S.sfree[st]);  // the B stage served all home chunks
       }
-      ++tile;
+      ++mt;
+      if (last_g) {
+        g = 0;
+        ++tile;
+      } else {
+        ++g;
+      }
     }
     stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
+    if (T.prof && lane == 0) {
+      atomicAdd(&T.ctr->prof[5], (unsigned long long)ew_dfull);
+      atomicAdd(&T.ctr->prof[6], (unsigned long long)(clock64() - e_start));
+    }
     const uint32_t bt = __shfl_sync(FULL_MASK, warp_scan_incl(band_cnt), 31);
     const uint32_t at = __shfl_sync(FULL_MASK, warp_scan_incl(amb_cnt), 31);
     if (lane == 0) {
@@ -678,23 +729,24 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
 template <int KP>
 void launch_tc(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
   constexpr int NS = KP <= 64 ? 3 : 2;
-  const size_t dyn = (2 + 2 * NS) * (size_t)TM * KP * sizeof(__nv_bfloat16) +
+  constexpr int G = KP <= 32 ? 2 : 1;  // home chunks per unit (must match tc_rows)
+  const size_t dyn = (2 * G + 2 * NS) * (size_t)TM * KP * sizeof(__nv_bfloat16) +
                      (size_t)4 * 32 * SV_STRIDE * sizeof(float) + 4 * PSTAGE * sizeof(unsigned long long);
-  MCK(cudaFuncSetAttribute(k_join_tc<KP, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-  MCK(cudaFuncSetAttribute(k_join_tc<KP, NS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  MCK(cudaFuncSetAttribute(k_join_tc<KP, NS, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  MCK(cudaFuncSetAttribute(k_join_tc<KP, NS, G>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
-  MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join_tc<KP, NS>, TC_THREADS2, dyn));
+  MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join_tc<KP, NS, G>, TC_THREADS2, dyn));
   if (per_sm < 1) throw Error(MISTIC_ERR_TOO_LARGE, "tensor-core join does not fit on an SM");
   const int occ = per_sm;
   // two CTAs per SM: 256 TMEM columns each (512 per SM), and registers and
   // shared memory allow two for every KP <= 64; the occupancy query reports
   // one for this 9-warp block, so it only serves as the fits-at-all check
-  per_sm = KP <= 64 ? 2 : 1;
+  per_sm = (dyn + sizeof(TcShared2<NS, G>) + 1024) * 2 <= 228 * 1024 ? 2 : 1;
   const unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)per_sm * h->sms, T.n_units);
   if (getenv("MISTIC_DEBUG"))
     fprintf(stderr, "[mistic] join_tc KP=%d NS=%d dyn=%zu occupancy=%d grid=%u units=%llu\n", KP, NS, dyn, occ, grid,
             (unsigned long long)T.n_units);
-  k_join_tc<KP, NS><<<grid, TC_THREADS2, dyn, h->stream>>>(P, T);
+  k_join_tc<KP, NS, G><<<grid, TC_THREADS2, dyn, h->stream>>>(P, T);
   launched(h, "join_tc");
 }
 
@@ -703,6 +755,9 @@ void launch_tc(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
 namespace join {
 
 int tc_kp(uint32_t d) { return (int)(((d + 2) + 15) / 16 * 16); }
+// Home rows per tensor-core unit: G chunks of 128 share each converted
+// candidate tile (G = 2 while the operands leave room for two CTAs per SM).
+uint32_t tc_rows(uint32_t d) { return tc_kp(d) <= 32 ? 2 * TM : TM; }
 bool tc_supported(uint32_t d) { return tc_kp(d) <= 128; }
 
 void run_tc(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {

@@ -406,7 +406,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   ep.chunk = (uint32_t)CH;
   ep.seg_cap = 4096;
   ep.tc_min = use_tc ? tc_min_bin() : 0u;
-  ep.tc_chunk = 128;
+  ep.tc_chunk = use_tc ? join::tc_rows(d) : 128;
   uint32_t* nbr_cnt = abuf<uint32_t>(h, "nbr_cnt", m + 1);
   uint32_t* unit_cnt = abuf<uint32_t>(h, "unit_cnt", m + 1);
   uint32_t* unit_cnt_tc = abuf<uint32_t>(h, "unit_cnt_tc", m + 1);
@@ -479,6 +479,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     const char* st = getenv("MISTIC_TEST_TC_STALL");
     tp.stall_test = (st && *st == '1') ? 1 : 0;
     tp.wait_limit = tp.stall_test ? (1ll << 12) : (1ll << 22);
+    tp.prof = getenv("MISTIC_DEBUG") ? 1 : 0;
   }
   const bool want_pairs = o.pairs != MISTIC_PAIRS_NONE;
   const bool want_csr = o.csr != MISTIC_PAIRS_NONE;
@@ -526,6 +527,14 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     d2h(h, &tcc, ctr + 1, sizeof tcc);
     r->tc_tiles = tcc.tiles;
     r->tc_cells = tcc.cells;
+    if (tp.prof) {
+      const double tot_p = (double)tcc.prof[1], tot_m = (double)tcc.prof[4], tot_e = (double)tcc.prof[6];
+      fprintf(stderr,
+              "[mistic] join_tc roles: producers wait-for-free-stage %.1f%% | MMA wait-full %.1f%% wait-free-acc "
+              "%.1f%% | epilogue wait-acc %.1f%%\n",
+              tot_p ? 100.0 * tcc.prof[0] / tot_p : 0.0, tot_m ? 100.0 * tcc.prof[2] / tot_m : 0.0,
+              tot_m ? 100.0 * tcc.prof[3] / tot_m : 0.0, tot_e ? 100.0 * tcc.prof[5] / tot_e : 0.0);
+    }
   }
 
   // ---- CSR neighbour table (from the packed pair list, before it is sorted or converted)
