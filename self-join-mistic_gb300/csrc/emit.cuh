@@ -52,8 +52,15 @@ __device__ __forceinline__ void stage_flush(PairStage& ps, unsigned long long* c
 template <class F>
 __device__ __forceinline__ void stage_pairs(PairStage& ps, uint32_t cnt, F pair_of, unsigned long long* counter,
                                             unsigned long long* pairs, unsigned long long cap) {
-  const uint32_t incl = stage_scan(cnt);
-  const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+  uint32_t incl, total;
+  if (__ballot_sync(FULL_MASK, cnt > 1) == 0) {  // at most one pair per lane: prefix by ballot
+    const uint32_t m1 = __ballot_sync(FULL_MASK, cnt != 0);
+    incl = __popc(m1 & (0xffffffffu >> (31 - (threadIdx.x & 31))));
+    total = __popc(m1);
+  } else {
+    incl = stage_scan(cnt);
+    total = __shfl_sync(FULL_MASK, incl, 31);
+  }
   if (total == 0) return;
   if (ps.n + total > PSTAGE) stage_flush(ps, counter, pairs, cap);
   if (total > PSTAGE) {  // a dense block: reserve directly

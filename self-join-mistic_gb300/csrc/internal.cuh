@@ -77,7 +77,8 @@ struct JoinCounters {
   unsigned long long error;      // non-zero: a bounded device wait gave up
   unsigned long long tiles;      // tensor-core tiles evaluated
   unsigned long long cells;      // sum over those tiles of home rows x candidate columns
-  unsigned long long prof[8];    // role cycle breakdown when TcParams.prof is set
+  unsigned long long band_n;     // candidate pairs appended to the band list (decided afterwards in FP64)
+  unsigned long long prof[16];   // role cycle breakdown when TcParams.prof is set
 };
 
 // Key packing: field f = floor((D[i*kstride + col[f]] - dmin[f]) / w[f]),
@@ -119,6 +120,8 @@ struct JoinParams {
   double amb;           // 4 ulp(eps2)
   unsigned long long* pairs;  // packed (i << 32 | j), i < j; null when counting only
   unsigned long long cap;
+  unsigned long long* band_list;  // packed (i << 32 | j) original ids whose fast value is inside the error band
+  unsigned long long band_cap;
   JoinCounters* ctr;
 };
 
@@ -208,6 +211,8 @@ bool filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_
 namespace join {
 int chunk_for(bool fp64, uint32_t dpad);
 void run(mistic_handle_s*, bool fp64, int CH, const JoinParams&);
+// FP64 decision of the band list left by the FP32 / tensor-core joins.
+void run_band(mistic_handle_s*, const JoinParams&);
 // Tensor-core join over TcParams.units; KP = augmented K (d + 2 rounded up to 16).
 bool tc_supported(uint32_t d);
 int tc_kp(uint32_t d);

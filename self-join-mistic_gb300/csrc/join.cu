@@ -47,28 +47,43 @@ __device__ __forceinline__ uint32_t warp_incl_scan_u32(uint32_t x) {
 // subtraction, product and sum rounded to FP64 (no contraction).
 __device__ __forceinline__ double exact_sqdist(const JoinParams& P, uint32_t i, uint32_t j) {
   double s = 0.0;
-  if (P.raw_f32) {
-    const float* a = (const float*)P.raw + (size_t)i * P.d;
-    const float* b = (const float*)P.raw + (size_t)j * P.d;
-    for (uint32_t t = 0; t < P.d; ++t) {
-      double df = __dsub_rn((double)a[t], (double)b[t]);
-      s = __dadd_rn(s, __dmul_rn(df, df));
+  // loads in groups of 8 (all in flight), sums in coordinate order
+  for (uint32_t t0 = 0; t0 < P.d; t0 += 8) {
+    double av[8], bv[8];
+    if (P.raw_f32) {
+      const float* a = (const float*)P.raw + (size_t)i * P.d;
+      const float* b = (const float*)P.raw + (size_t)j * P.d;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        av[k] = t0 + k < P.d ? (double)a[t0 + k] : 0.0;
+        bv[k] = t0 + k < P.d ? (double)b[t0 + k] : 0.0;
+      }
+    } else {
+      const double* a = (const double*)P.raw + (size_t)i * P.d;
+      const double* b = (const double*)P.raw + (size_t)j * P.d;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        av[k] = t0 + k < P.d ? a[t0 + k] : 0.0;
+        bv[k] = t0 + k < P.d ? b[t0 + k] : 0.0;
+      }
     }
-  } else {
-    const double* a = (const double*)P.raw + (size_t)i * P.d;
-    const double* b = (const double*)P.raw + (size_t)j * P.d;
-    for (uint32_t t = 0; t < P.d; ++t) {
-      double df = __dsub_rn(a[t], b[t]);
-      s = __dadd_rn(s, __dmul_rn(df, df));
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (t0 + k < P.d) {
+        const double df = __dsub_rn(av[k], bv[k]);
+        s = __dadd_rn(s, __dmul_rn(df, df));
+      }
     }
   }
   return s;
 }
 
-// Stages this lane's accepted pairs (bit a of `acc`: home point a0 + a with
-// candidate q) through the warp's buffer.
-__device__ __forceinline__ void stage_hits(PairStage& ps, const JoinParams& P, uint32_t acc, uint32_t a0,
-                                           uint32_t q) {
+// Stages this lane's pairs (bit a of `acc`: home point a0 + a with
+// candidate q) through the warp's buffer into a pair list (accepted pairs,
+// or the band list of pairs to re-decide in FP64).
+__device__ __forceinline__ void stage_hits(PairStage& ps, const JoinParams& P, uint32_t acc, uint32_t a0, uint32_t q,
+                                           unsigned long long* counter, unsigned long long* list,
+                                           unsigned long long cap) {
   const uint32_t iq = acc ? P.ids[q] : 0u;
   uint32_t bits = acc;
   stage_pairs(
@@ -80,7 +95,7 @@ __device__ __forceinline__ void stage_hits(PairStage& ps, const JoinParams& P, u
         const uint32_t lo = ia < iq ? ia : iq, hi = ia < iq ? iq : ia;
         return ((unsigned long long)lo << 32) | hi;
       },
-      &P.ctr->pairs, P.pairs, P.cap);
+      counter, list, cap);
 }
 
 __device__ __forceinline__ void add_counter(unsigned long long* c, uint32_t v) {
@@ -206,9 +221,10 @@ k_join_f32(const JoinParams P) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t nq4 = P.dpad >> 2;
   float4* sA = smem_f4 + (size_t)w * CH * nq4;
-  PairStage ps{reinterpret_cast<unsigned long long*>(smem_f4 + (size_t)(blockDim.x >> 5) * CH * nq4) + (size_t)w * PSTAGE, 0};
+  unsigned long long* stg = reinterpret_cast<unsigned long long*>(smem_f4 + (size_t)(blockDim.x >> 5) * CH * nq4);
+  PairStage ps{stg + (size_t)w * PSTAGE, 0};
+  PairStage bs{stg + (size_t)((blockDim.x >> 5) + w) * PSTAGE, 0};
   const float4* X = (const float4*)P.xs;
-  uint32_t band_cnt = 0, amb_cnt = 0;
   for (;;) {
     unsigned long long u = 0;
     if (lane == 0) u = atomicAdd(&P.ctr->next_unit, 1ull);
@@ -244,25 +260,15 @@ k_join_f32(const JoinParams P) {
           lo_m |= (acc[a] <= P.t_lo ? 1u : 0u) << a;
         }
         lo_m &= m;
-        uint32_t band = m & ~lo_m, acc_m = lo_m;
-        if (band) {
-          const uint32_t iq = P.ids[q];
-          while (band) {
-            const int a = __ffs(band) - 1;
-            band &= band - 1;
-            const double sd = exact_sqdist(P, P.ids[a0 + a], iq);
-            ++band_cnt;
-            if (fabs(sd - P.eps2) <= P.amb) ++amb_cnt;
-            if (sd <= P.eps2) acc_m |= 1u << a;
-          }
-        }
-        stage_hits(ps, P, acc_m, a0, q);
+        const uint32_t band = m & ~lo_m;
+        stage_hits(ps, P, lo_m, a0, q, &P.ctr->pairs, P.pairs, P.cap);
+        if (__any_sync(FULL_MASK, band != 0u))  // decided later, all at once (k_band_check)
+          stage_hits(bs, P, band, a0, q, &P.ctr->band_n, P.band_list, P.band_cap);
       }
     }
   }
   stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
-  add_counter(&P.ctr->band, band_cnt);
-  add_counter(&P.ctr->ambiguous, amb_cnt);
+  stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap);
 }
 
 // FP32 filter for d <= 32: the lane's candidate row lives in registers as DQ
@@ -276,9 +282,10 @@ k_join_f32r(const JoinParams P) {
   extern __shared__ float4 smem_f4r[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   float4* sA = smem_f4r + (size_t)w * CH * DQ;
-  PairStage ps{reinterpret_cast<unsigned long long*>(smem_f4r + (size_t)(blockDim.x >> 5) * CH * DQ) + (size_t)w * PSTAGE, 0};
+  unsigned long long* stg = reinterpret_cast<unsigned long long*>(smem_f4r + (size_t)(blockDim.x >> 5) * CH * DQ);
+  PairStage ps{stg + (size_t)w * PSTAGE, 0};
+  PairStage bs{stg + (size_t)((blockDim.x >> 5) + w) * PSTAGE, 0};
   const float4* X = (const float4*)P.xs;
-  uint32_t band_cnt = 0, amb_cnt = 0;
   for (;;) {
     unsigned long long u = 0;
     if (lane == 0) u = atomicAdd(&P.ctr->next_unit, 1ull);
@@ -328,25 +335,15 @@ k_join_f32r(const JoinParams P) {
       m = t.qv ? (m & home_mask(na, q >= hs && q < he, q, a0, CH)) : 0u;
       if (__any_sync(FULL_MASK, m != 0)) {
         lo_m &= m;
-        uint32_t band = m & ~lo_m, acc_m = lo_m;
-        if (band) {
-          const uint32_t iq = P.ids[q];
-          while (band) {
-            const int a = __ffs(band) - 1;
-            band &= band - 1;
-            const double sd = exact_sqdist(P, P.ids[a0 + a], iq);
-            ++band_cnt;
-            if (fabs(sd - P.eps2) <= P.amb) ++amb_cnt;
-            if (sd <= P.eps2) acc_m |= 1u << a;
-          }
-        }
-        stage_hits(ps, P, acc_m, a0, q);
+        const uint32_t band = m & ~lo_m;
+        stage_hits(ps, P, lo_m, a0, q, &P.ctr->pairs, P.pairs, P.cap);
+        if (__any_sync(FULL_MASK, band != 0u))  // decided later, all at once (k_band_check)
+          stage_hits(bs, P, band, a0, q, &P.ctr->band_n, P.band_list, P.band_cap);
       }
     }
   }
   stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
-  add_counter(&P.ctr->band, band_cnt);
-  add_counter(&P.ctr->ambiguous, amb_cnt);
+  stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap);
 }
 
 // ---------------------------------------------------------------- FP64 plain
@@ -428,7 +425,7 @@ k_join_f64(const JoinParams P) {
         }
         acc_m &= m;
         amb_cnt += __popc(amb_m & m);
-        stage_hits(ps, P, acc_m, a0, q);
+        stage_hits(ps, P, acc_m, a0, q, &P.ctr->pairs, P.pairs, P.cap);
       }
     }
   }
@@ -437,7 +434,50 @@ k_join_f64(const JoinParams P) {
 }
 
 // ---------------------------------------------------------------- launcher
+// ---------------------------------------------------------------- band check
+// The FP32 and tensor-core joins append pairs whose fast value falls inside
+// the error band to P.band_list; this pass decides them with the reference
+// FP64 predicate, one pair per thread, and appends the accepted ones (same
+// packing) to the pair list.  The list length is read on the device.
+__global__ void __launch_bounds__(256) k_band_check(const JoinParams P) {
+  const unsigned long long n = min(*(volatile unsigned long long*)&P.ctr->band_n, P.band_cap);
+  const int lane = threadIdx.x & 31;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  uint32_t cnt = 0, amb = 0;
+  for (unsigned long long i0 = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < n;
+       i0 += stride) {
+    const unsigned long long i = i0 + lane;
+    bool acc = false;
+    unsigned long long e = 0;
+    if (i < n) {
+      e = P.band_list[i];
+      const double sd = exact_sqdist(P, (uint32_t)(e >> 32), (uint32_t)e);
+      ++cnt;
+      if (fabs(sd - P.eps2) <= P.amb) ++amb;
+      acc = sd <= P.eps2;
+    }
+    const uint32_t m = __ballot_sync(FULL_MASK, acc);
+    if (m) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&P.ctr->pairs, (unsigned long long)__popc(m));
+      base = __shfl_sync(FULL_MASK, base, 0);
+      if (acc && P.pairs) {
+        const unsigned long long pos = base + __popc(m & ((1u << lane) - 1u));
+        if (pos < P.cap) P.pairs[pos] = e;
+      }
+    }
+  }
+  add_counter(&P.ctr->band, cnt);
+  add_counter(&P.ctr->ambiguous, amb);
+}
+
 namespace join {
+
+void run_band(mistic_handle_s* h, const JoinParams& P) {
+  if (!P.band_list) return;
+  k_band_check<<<(unsigned)h->sms * 8, 256, 0, h->stream>>>(P);
+  launched(h, "band_check");
+}
 
 // Home points per unit for a mode and padded width: 32 (FP32) / 16 (FP64)
 // while a warp's staged chunk stays within 16 KB, else 8 / 4.
@@ -452,7 +492,7 @@ template <class K>
 static void launch_persistent(mistic_handle_s* h, K kern, size_t smem_per_warp, const JoinParams& P,
                               const char* name) {
   constexpr size_t kBlockSmem = 200 * 1024;
-  smem_per_warp += PSTAGE * sizeof(unsigned long long);  // pair staging buffer
+  smem_per_warp += 2 * PSTAGE * sizeof(unsigned long long);  // pair and band staging buffers
   int warps = (int)std::min<size_t>(JOIN_THREADS / 32, std::max<size_t>(1, kBlockSmem / smem_per_warp));
   const size_t smem = smem_per_warp * warps;
   if (smem > kBlockSmem + 27 * 1024)

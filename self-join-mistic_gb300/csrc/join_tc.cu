@@ -52,7 +52,6 @@ constexpr int TM = 128;          // home rows per tile (MMA M)
 constexpr int TN = 128;          // candidate columns per tile (MMA N)
 constexpr int WIN = 256;         // neighbour bins per candidate window
 constexpr long long kWaitLimit = 1ll << 22;
-constexpr int SV_STRIDE = 36;    // per-lane scratch row (floats), 16-B aligned
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -92,26 +91,6 @@ __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&v)[3
 __device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 
-__device__ __forceinline__ double exact_sqdist_tc(const JoinParams& P, uint32_t i, uint32_t j) {
-  double s = 0.0;
-  if (P.raw_f32) {
-    const float* a = (const float*)P.raw + (size_t)i * P.d;
-    const float* b = (const float*)P.raw + (size_t)j * P.d;
-    for (uint32_t t = 0; t < P.d; ++t) {
-      const double df = __dsub_rn((double)a[t], (double)b[t]);
-      s = __dadd_rn(s, __dmul_rn(df, df));
-    }
-  } else {
-    const double* a = (const double*)P.raw + (size_t)i * P.d;
-    const double* b = (const double*)P.raw + (size_t)j * P.d;
-    for (uint32_t t = 0; t < P.d; ++t) {
-      const double df = __dsub_rn(a[t], b[t]);
-      s = __dadd_rn(s, __dmul_rn(df, df));
-    }
-  }
-  return s;
-}
-
 __device__ __forceinline__ uint32_t warp_scan_incl(uint32_t x) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -139,34 +118,42 @@ __device__ __forceinline__ uint32_t warp_scan_incl(uint32_t x) {
 //   dfree[b]  epilogue  -> MMA        (4 arrivals; accumulator b reusable)
 //   afull     producers -> MMA        (128 arrivals per unit: A written)
 //   afree     MMA       -> producers  (tcgen05.commit after a unit's last tile)
-constexpr int TC_WARPS = 9;
-constexpr int TC_THREADS2 = TC_WARPS * 32;
-constexpr int NPROD = 128;
+constexpr int NPW = 8;     // producer warps: two threads per operand row
+constexpr int NPROD = NPW * 32;
+// NEPI epilogue warps (a template parameter: 8 or 16) cover the 4 TMEM lane
+// quarters x NEPI / 4 column-block groups; the MMA warp follows them.
+constexpr int EPI0 = NPW;  // first epilogue warp (a multiple of 4: warp % 4 is its lane quarter)
+__host__ __device__ constexpr int tc_threads(int nepi) { return (EPI0 + nepi + 1) * 32; }
+constexpr int NACC = 4;    // TMEM accumulators of 128 columns (512 per CTA, one CTA per SM)
 constexpr uint32_t FLAG_FIRST = 1, FLAG_LAST = 2, FLAG_END = 4;
 
 struct TileMeta {
-  uint32_t a0, na, hs, he, ncols, flags, ng;  // ng: 128-row MMA tiles of this unit (1..G)
+  uint32_t a0, na, ncols, flags, ng;  // ng: 128-row MMA tiles of this unit (1..G)
+  uint32_t hcr, hq;  // columns [hcr & 255, hcr >> 8) hold home-bin rows, the first at sorted position hq
 };
 
-template <int NS, int G>
+template <int NS, int G, int RAW>
 struct TcShared2 {
-  __align__(16) float center[128];
-  uint32_t qpos[NS][TN];
+  __align__(16) float cadd_a[128];  // -c   (A rows: x - c)
+  __align__(16) float cadd_b[128];  // 2c   (B rows: -2 (x - c))
+  uint32_t w_home;  // (window generation << 8) | index of the home bin in the window
+  uint32_t hx[4][2];  // home column range of issued tiles (producer thread 0 only)
   uint32_t qid[NS][TN];      // original row ids of the candidates
   uint32_t aid[NS][TM * G];  // original row ids of the home rows (per stage: the epilogue
                              // may still read a finished unit while producers start the next)
   float dlt[NS][TN];  // accept when D' <= -dlt
   TileMeta meta[NS];
+  uint32_t rid[RAW > 0 ? RAW : 1][TN];  // candidate ids of the tiles in the raw ring
   uint32_t w_start[WIN];
   uint32_t w_pref[WIN + 1];
-  uint32_t scan_ws[4];
+  uint32_t scan_ws[NPW];
   unsigned long long unit;
   uint32_t w_total, w_pos, seg_next, w_nb;
   uint32_t ra2max;  // float bits, non-negative
   uint32_t abort_flag;
   uint32_t tmem_base;
-  uint32_t pflag;  // producer-wide decision, written by producer thread 0
-  unsigned long long full[NS], sfree[NS], dfull[2], dfree[2], afull, afree;
+  uint32_t pflag[2];  // producer-wide decisions, written by producer thread 0
+  unsigned long long full[NS], sfree[NS], dfull[NACC], dfree[NACC], afull, afree;
 };
 
 __device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count) {
@@ -179,7 +166,7 @@ __device__ __forceinline__ void tc_commit(unsigned long long* b) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(b))
                : "memory");
 }
-__device__ __forceinline__ void prod_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+__device__ __forceinline__ void prod_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NPROD) : "memory"); }
 
 // Bounded wait; on expiry raise the CTA's abort flag.  Returns false if the
 // CTA is aborting (now or already).
@@ -198,86 +185,128 @@ __device__ __forceinline__ bool wait_or_abort(unsigned long long* b, uint32_t pa
   return false;
 }
 
-// One augmented operand row, hi and lo parts.  k < d: scale * (x[k] - c[k]);
-// A rows (is_a): [.., |a'|^2, 1]; B rows: [.., 1, |q'|^2 - tcol].
-// FP32 norm of the centred row, sum over k < d of (x[k] - c[k])^2.  The
-// row is read in groups of 8 float4 with all loads of a group in flight.
-__device__ __forceinline__ float row_norm(const float* __restrict__ x, const float* c, uint32_t d, uint32_t dpad) {
-  float nrm = 0.f;
-  for (uint32_t g = 0; g < dpad; g += 32) {
-    float4 xv[8];
+// Operand rows live in the no-swizzle K-major core-matrix layout: the
+// 16-byte chunk of row r and K block kb (8 bf16) sits at bf16 offset
+// chunk_off(r, kb).  A raw FP32 row is first copied (cp.async) into the
+// chunk slots of the row itself -- floats [8kb, 8kb+4) into the hi chunk of
+// block kb, [8kb+4, 8kb+8) into its lo chunk -- and then converted in place,
+// block by block, into the augmented bf16 hi/lo row.  Two threads share a
+// row, one per half of the K blocks; a thread only touches its own chunks.
+template <int KP>
+__device__ __forceinline__ uint32_t chunk_off(uint32_t r, uint32_t kb) {
+  return ((r >> 3) * (KP / 8) + kb) * 64 + (r & 7) * 8;
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+template <int KP>
+__device__ __forceinline__ void load_half(__nv_bfloat16* hi, __nv_bfloat16* lo, uint32_t r, uint32_t half,
+                                          const float* __restrict__ xr, uint32_t dpad) {
+  constexpr int HB = KP / 16;
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
-      xv[i] = g + 4 * i < dpad ? *reinterpret_cast<const float4*>(x + g + 4 * i) : make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int j = 0; j < HB; ++j) {
+    const uint32_t kb = half * HB + j, k0 = 8 * kb, off = chunk_off<KP>(r, kb);
+    if (k0 < dpad) cp_async16(hi + off, xr + k0);
+    if (k0 + 4 < dpad) cp_async16(lo + off, xr + k0 + 4);
+  }
+}
+
+__device__ __forceinline__ void unpack8(const __nv_bfloat16* hi, const __nv_bfloat16* lo, uint32_t off, bool l0,
+                                        bool l1, float (&x)[8]) {
+  float4 x0 = make_float4(0.f, 0.f, 0.f, 0.f), x1 = x0;
+  if (l0) x0 = *reinterpret_cast<const float4*>(hi + off);
+  if (l1) x1 = *reinterpret_cast<const float4*>(lo + off);
+  x[0] = x0.x, x[1] = x0.y, x[2] = x0.z, x[3] = x0.w;
+  x[4] = x1.x, x[5] = x1.y, x[6] = x1.z, x[7] = x1.w;
+}
+
+__device__ __forceinline__ void store_split(__nv_bfloat16* hi, __nv_bfloat16* lo, uint32_t off, const float (&v)[8]) {
+  uint4 oh, ol;
+  uint32_t* ph = reinterpret_cast<uint32_t*>(&oh);
+  uint32_t* pl = reinterpret_cast<uint32_t*>(&ol);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const uint32_t k = g + 4 * i;
-      const float4 cv = k < dpad ? *reinterpret_cast<const float4*>(c + k) : make_float4(0.f, 0.f, 0.f, 0.f);
-      const float xs[4] = {xv[i].x, xv[i].y, xv[i].z, xv[i].w}, cs[4] = {cv.x, cv.y, cv.z, cv.w};
+  for (int i = 0; i < 4; ++i) {
+    const __nv_bfloat162 hv = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+    const float2 hf = __bfloat1622float2(hv);
+    const __nv_bfloat162 lv = __floats2bfloat162_rn(v[2 * i] - hf.x, v[2 * i + 1] - hf.y);
+    ph[i] = *reinterpret_cast<const uint32_t*>(&hv);
+    pl[i] = *reinterpret_cast<const uint32_t*>(&lv);
+  }
+  *reinterpret_cast<uint4*>(hi + off) = oh;
+  *reinterpret_cast<uint4*>(lo + off) = ol;
+}
+
+// Operand values: scale * fl(x[k] - c[k]) = fma(x[k], scale, cadd[k]) with
+// cadd = -scale * c, exactly (scale is 1 or -2).  The row norm |x - c|^2 is
+// accumulated from the scaled values (fma(v, v, acc) = scale^2 fma(t, t, acc')
+// exactly) in K order per half; the halves are added by the caller.
+//
+// Pass 1 writes every K block of this thread except the (at most two)
+// blocks that hold the augmented columns d, d + 1, and returns the partial
+// sum of v^2; pass 2 writes those blocks once the norm is known.  A block
+// is read before it is written, so the source may be the destination.
+template <int KP>
+__device__ __forceinline__ float conv_pass1(const __nv_bfloat16* sh, const __nv_bfloat16* sl, __nv_bfloat16* hi,
+                                            __nv_bfloat16* lo, uint32_t r, uint32_t half, bool ok, const float* cadd,
+                                            float scale, uint32_t d) {
+  constexpr int HB = KP / 16;
+  float acc = 0.f;
+#pragma unroll 2
+  for (int j = 0; j < HB; ++j) {
+    const uint32_t kb = half * HB + j, k0 = 8 * kb, off = chunk_off<KP>(r, kb);
+    float v[8];
+    if (!ok || k0 >= d + 2) {  // zero block
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        if (k + j < d) {
-          const float t = xs[j] - cs[j];
-          nrm = fmaf(t, t, nrm);
+      for (int i = 0; i < 8; ++i) v[i] = 0.f;
+      store_split(hi, lo, off, v);
+      continue;
+    }
+    float x[8];
+    unpack8(sh, sl, off, true, k0 + 4 < d, x);
+    if (k0 + 8 <= d) {  // full block
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        v[i] = fmaf(x[i], scale, cadd[k0 + i]);
+        acc = fmaf(v[i], v[i], acc);
+      }
+      store_split(hi, lo, off, v);
+    } else {  // holds d or d + 1: norm part only
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        if (k0 + i < d) {
+          const float t = fmaf(x[i], scale, cadd[k0 + i]);
+          acc = fmaf(t, t, acc);
         }
       }
     }
   }
-  return nrm;
+  return acc;
 }
 
 template <int KP>
-__device__ __forceinline__ void write_row2(__nv_bfloat16* hi_base, __nv_bfloat16* lo_base, uint32_t r,
-                                           const float* __restrict__ x, const float* c, uint32_t d, uint32_t dpad,
-                                           bool is_a, float nrm, float tcol_in) {
-  const float tcol = is_a ? 0.f : tcol_in;
-  const float ed = is_a ? nrm : 1.f;
-  const float ed1 = is_a ? 1.f : nrm - tcol;
-  const float scale = is_a ? 1.f : -2.f;
+__device__ __forceinline__ void conv_pass2(const __nv_bfloat16* sh, const __nv_bfloat16* sl, __nv_bfloat16* hi,
+                                           __nv_bfloat16* lo, uint32_t r, uint32_t half, bool ok, const float* cadd,
+                                           float scale, uint32_t d, float e_d, float e_d1) {
+  constexpr int HB = KP / 16;
+  if (!ok) return;
+#pragma unroll 1
+  for (int j = 0; j < HB; ++j) {
+    const uint32_t kb = half * HB + j, k0 = 8 * kb, off = chunk_off<KP>(r, kb);
+    if (k0 + 8 <= d || k0 >= d + 2) continue;
+    float x[8], v[8];
+    unpack8(sh, sl, off, k0 < d, k0 + 4 < d, x);
 #pragma unroll
-  for (int kb = 0; kb < KP / 8; ++kb) {
-    float v[8];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const uint32_t k4 = kb * 8 + h * 4;
-      float4 xv = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (k4 < dpad) xv = *reinterpret_cast<const float4*>(x + k4);
-      const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const uint32_t k = k4 + i;
-        float t = 0.f;
-        if (k < d) t = (xs[i] - c[k]) * scale;
-        if (k == d) t = ed;
-        if (k == d + 1) t = ed1;
-        v[h * 4 + i] = t;
-      }
+    for (int i = 0; i < 8; ++i) {
+      const uint32_t k = k0 + i;
+      float t = 0.f;
+      if (k < d) t = fmaf(x[i], scale, cadd[k]);
+      if (k == d) t = e_d;
+      if (k == d + 1) t = e_d1;
+      v[i] = t;
     }
-    uint4 oh, ol;
-    uint32_t* ph = reinterpret_cast<uint32_t*>(&oh);
-    uint32_t* pl = reinterpret_cast<uint32_t*>(&ol);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const __nv_bfloat162 hv = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-      const float2 hf = __bfloat1622float2(hv);
-      const __nv_bfloat162 lv = __floats2bfloat162_rn(v[2 * i] - hf.x, v[2 * i + 1] - hf.y);
-      ph[i] = *reinterpret_cast<const uint32_t*>(&hv);
-      pl[i] = *reinterpret_cast<const uint32_t*>(&lv);
-    }
-    const uint32_t off = (((r >> 3) * (KP / 8) + kb) * 64) + (r & 7) * 8;
-    *reinterpret_cast<uint4*>(hi_base + off) = oh;
-    *reinterpret_cast<uint4*>(lo_base + off) = ol;
-  }
-}
-
-template <int KP>
-__device__ __forceinline__ void zero_row2(__nv_bfloat16* hi_base, __nv_bfloat16* lo_base, uint32_t r) {
-  const uint4 z = make_uint4(0, 0, 0, 0);
-#pragma unroll
-  for (int kb = 0; kb < KP / 8; ++kb) {
-    const uint32_t off = (((r >> 3) * (KP / 8) + kb) * 64) + (r & 7) * 8;
-    *reinterpret_cast<uint4*>(hi_base + off) = z;
-    *reinterpret_cast<uint4*>(lo_base + off) = z;
+    store_split(hi, lo, off, v);
   }
 }
 
@@ -301,16 +330,18 @@ __device__ __forceinline__ bool column_threshold(const TcParams& T, float ra2max
   return true;
 }
 
-template <int KP, int NS, int G>
-__global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, const TcParams T) {
+template <int KP, int NS, int G, int RAW, int NEPI>
+__global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParams P, const TcParams T) {
+  constexpr int MMA_WARP = EPI0 + NEPI;
   extern __shared__ __align__(128) unsigned char tc_dyn[];
-  __shared__ TcShared2<NS, G> S;
+  __shared__ TcShared2<NS, G, RAW> S;
   constexpr uint32_t OPB = TM * KP;  // bf16 elements per operand buffer
   __nv_bfloat16* Ahi = reinterpret_cast<__nv_bfloat16*>(tc_dyn);  // G home chunks of 128 rows
   __nv_bfloat16* Alo = Ahi + G * OPB;
   __nv_bfloat16* Bhi = Alo + G * OPB;  // NS stages of hi, then NS stages of lo
   __nv_bfloat16* Blo = Bhi + NS * OPB;
-  float* sv = reinterpret_cast<float*>(Blo + NS * OPB);  // 4 epilogue warps x 32 lanes x SV_STRIDE
+  __nv_bfloat16* Raw = Blo + NS * OPB;  // RAW landing slots (raw FP32 rows in the chunk layout, 2 * OPB each)
+  unsigned long long* pstage = reinterpret_cast<unsigned long long*>(Raw + RAW * 2 * OPB);  // 2 NEPI x PSTAGE
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const float* X = (const float*)P.xs;
   volatile uint32_t* abort_flag = &S.abort_flag;
@@ -318,19 +349,20 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
   if (tid == 0) {
     for (int i = 0; i < NS; ++i) {
       mbar_init(&S.full[i], NPROD);
-      mbar_init(&S.sfree[i], 4);
+      mbar_init(&S.sfree[i], NEPI);
     }
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < NACC; ++i) {
       mbar_init(&S.dfull[i], 1);
-      mbar_init(&S.dfree[i], 4);
+      mbar_init(&S.dfree[i], NEPI);
     }
     mbar_init(&S.afull, NPROD);
     mbar_init(&S.afree, 1);
     asm volatile("fence.mbarrier_init.release.cluster;");
     S.abort_flag = 0;
+    S.w_home = 0xffffffffu;
   }
-  if (warp == 8) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&S.tmem_base)));
+  if (warp == MMA_WARP) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&S.tmem_base)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -338,15 +370,23 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tbase = S.tmem_base;
 
-  if (warp < 4) {
-    // ============================ producers
-    // Every branch that leads to bar.sync is taken on a value all 128
-    // producer threads read from shared memory after the same bar.sync, so
-    // the 4 warps never diverge around it; barrier waits are done by thread 0
-    // and broadcast through S.pflag.
-    uint32_t tile = 0, unit_k = 0;
+  if (warp < NPW) {
+    // ============================ producers (NPW warps, two threads per row)
+    // Thread (prow, half): row prow = 16 * warp + lane % 16 of every operand
+    // tile, K blocks [half * KP/16, (half + 1) * KP/16).  Every branch that
+    // leads to bar.sync is taken on a value all producer threads hold in
+    // registers or read from shared memory after the same bar.sync; barrier
+    // waits are done by thread 0 and broadcast through S.pflag[2] (two slots:
+    // a thread is at most one bar.sync behind thread 0).
+    const uint32_t prow = ((uint32_t)warp << 4) | (lane & 15), half = lane >> 4;
+    uint32_t tile = 0, issued = 0, unit_k = 0, pf = 0;
     unsigned long long n_tiles = 0, n_cells = 0;
-    long long pw_sfree = 0;
+    long long pw_sfree = 0, pc_unit = 0, pc_win = 0, pc_conv = 0, pc_ldw = 0;
+    uint32_t wgen = 0;  // window refills so far (tags S.w_home)
+    // tiles in flight: RAW landing slots, or (rows landing in the B stages
+    // themselves) NS - 1, so that issuing tile t + LA - 1 waits only on tiles
+    // before t
+    constexpr uint32_t LA = RAW > 0 ? RAW : (NS - 1 < 3 ? NS - 1 : 3);
     const long long p_start = T.prof ? clock64() : 0;
     auto end_marker = [&]() {  // last tile slot: tells the MMA warp and the epilogue to stop
       const uint32_t st = tile % NS;
@@ -358,15 +398,17 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
       mbar_arrive(&S.full[st]);
     };
     for (;;) {
+      const long long cu0 = T.prof ? clock64() : 0;
+      const uint32_t slot = pf++ & 1;
       if (tid == 0) {
         const unsigned long long uu = atomicAdd(&T.ctr->next_unit, 1ull);
         S.unit = uu;
         bool go = uu < T.n_units && !*abort_flag;
         if (go && unit_k > 0) go = wait_or_abort(&S.afree, (unit_k - 1) & 1, abort_flag, T.wait_limit);  // A no longer read
-        S.pflag = go ? 1u : 0u;
+        S.pflag[slot] = go ? 1u : 0u;
       }
       prod_sync();
-      if (!S.pflag) {
+      if (!S.pflag[slot]) {
         end_marker();
         break;
       }
@@ -376,24 +418,33 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
       const uint32_t a0 = hs + U.chunk * (TM * G);
       const uint32_t na = min((uint32_t)(TM * G), he - a0);
       const uint32_t ng = (na + TM - 1) / TM;
-      if (tid < (int)P.dpad) S.center[tid] = X[(size_t)a0 * P.dpad + tid];
+      if (tid < (int)P.dpad) {
+        const float c = X[(size_t)a0 * P.dpad + tid];
+        S.cadd_a[tid] = -c;
+        S.cadd_b[tid] = 2.f * c;
+      }
       if (tid == 0) S.ra2max = 0;
       prod_sync();
-      uint32_t my_aid[G];  // original ids of home rows tid, 128 + tid, ...
+      uint32_t my_aid[(G + 1) / 2];  // original ids of home rows g * TM + prow, g = half, half + 2, ...
 #pragma unroll
-      for (int g = 0; g < G; ++g) my_aid[g] = (uint32_t)(g * TM + tid) < na ? P.ids[a0 + g * TM + tid] : 0u;
+      for (int i = 0; i < (G + 1) / 2; ++i) {
+        const uint32_t r = (2 * i + half) * TM + prow;
+        my_aid[i] = (2 * i + (int)half < G && r < na) ? P.ids[a0 + r] : 0u;
+      }
       {
+        for (uint32_t g = 0; g < ng; ++g) {
+          const uint32_t r = g * TM + prow;
+          if (r < na) load_half<KP>(Ahi + g * OPB, Alo + g * OPB, prow, half, X + (size_t)(a0 + r) * P.dpad, P.dpad);
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
         float m = 0.f;
         for (uint32_t g = 0; g < ng; ++g) {
-          const uint32_t r = g * TM + tid;
-          if (r < na) {
-            const float* xr = X + (size_t)(a0 + r) * P.dpad;
-            const float nrm = row_norm(xr, S.center, P.d, P.dpad);
-            write_row2<KP>(Ahi + g * OPB, Alo + g * OPB, tid, xr, S.center, P.d, P.dpad, true, nrm, 0.f);
-            m = fmaxf(m, nrm);
-          } else {
-            zero_row2<KP>(Ahi + g * OPB, Alo + g * OPB, tid);
-          }
+          const bool ok = g * TM + prow < na;
+          __nv_bfloat16 *ah = Ahi + g * OPB, *al = Alo + g * OPB;
+          const float part = conv_pass1<KP>(ah, al, ah, al, prow, half, ok, S.cadd_a, 1.f, P.d);
+          const float nrm = part + __shfl_xor_sync(FULL_MASK, part, 16);
+          conv_pass2<KP>(ah, al, ah, al, prow, half, ok, S.cadd_a, 1.f, P.d, nrm, 1.f);
+          m = fmaxf(m, ok ? nrm : 0.f);
         }
 #pragma unroll
         for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL_MASK, m, o));
@@ -401,117 +452,180 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&S.afull);
-      if (tid == 0) {
-        S.seg_next = U.s0;
-        S.w_total = 0;
-        S.w_pos = 0;
-      }
       prod_sync();
       const float ra2max = __uint_as_float(S.ra2max);
-      bool first = true, aborted = false;
-      for (;;) {
-        if (S.w_pos >= S.w_total) {
-          const uint32_t sn = S.seg_next;
-          if (sn >= U.s1) break;
-          const uint32_t nb = min((uint32_t)WIN, U.s1 - sn);
-          // 128 producer threads load up to 256 bins: two per thread
-          uint32_t st0 = 0, sz0 = 0, st1 = 0, sz1 = 0;
-          const uint32_t j0 = 2 * tid, j1 = 2 * tid + 1;
-          if (j0 < nb) {
-            const uint32_t b = P.nbr[sn + j0];
-            st0 = P.bstart[b];
-            sz0 = P.bstart[b + 1] - st0;
+      if (T.prof) pc_unit += clock64() - cu0;
+
+      // ---- candidate tiles of this unit: window of up to WIN neighbour bins
+      // (state uniform, in registers); the rows of up to LA tiles are in
+      // flight (cp.async, one group per tile) while the oldest is converted
+      uint32_t seg_next = U.s0, w_nb = 0, w_pos = 0, w_total = 0;
+      uint32_t pq = 0;  // (columns | last << 8) of the tiles in flight, 9 bits each, oldest lowest
+      int w_hj = -1;    // index of the home bin in the window, or -1
+      // 1: tile issued; 2: abort
+      auto advance = [&]() -> int {
+        while (w_pos >= w_total) {  // the caller checked that the unit has more tiles
+          const long long cw0 = T.prof ? clock64() : 0;
+          const uint32_t nb = min((uint32_t)WIN, U.s1 - seg_next);
+          uint32_t st0 = 0, sz0 = 0, bn = 0xffffffffu;
+          if ((uint32_t)tid < nb) {
+            bn = P.nbr[seg_next + tid];
+            st0 = P.bstart[bn];
+            sz0 = P.bstart[bn + 1] - st0;
           }
-          if (j1 < nb) {
-            const uint32_t b = P.nbr[sn + j1];
-            st1 = P.bstart[b];
-            sz1 = P.bstart[b + 1] - st1;
-          }
-          const uint32_t pair = sz0 + sz1;
-          const uint32_t incl = warp_scan_incl(pair);
+          const uint32_t incl = warp_scan_incl(sz0);
           if (lane == 31) S.scan_ws[warp] = incl;
           prod_sync();
           uint32_t wp = 0;
           for (int w = 0; w < warp; ++w) wp += S.scan_ws[w];
-          const uint32_t ex = wp + incl - pair;
-          if (j0 < nb) {
-            S.w_start[j0] = st0;
-            S.w_pref[j0 + 1] = ex + sz0;
+          ++wgen;
+          if ((uint32_t)tid < nb) {
+            S.w_start[tid] = st0;
+            S.w_pref[tid + 1] = wp + incl;
+            if (bn == U.h) S.w_home = ((wgen & 0xffffffu) << 8) | (uint32_t)tid;
           }
-          if (j1 < nb) {
-            S.w_start[j1] = st1;
-            S.w_pref[j1 + 1] = ex + sz0 + sz1;
-          }
-          if (tid == 0) {
-            S.w_pref[0] = 0;
-            S.w_nb = nb;
-            S.w_pos = 0;
-            S.seg_next = sn + nb;
-          }
+          if (tid == 0) S.w_pref[0] = 0;
           prod_sync();
-          if (tid == 0) S.w_total = S.w_pref[nb];
-          prod_sync();
-          continue;
+          {
+            const uint32_t wh = S.w_home;
+            w_hj = (wh >> 8) == (wgen & 0xffffffu) ? (int)(wh & 255u) : -1;
+          }
+          w_nb = nb;
+          w_pos = 0;
+          w_total = S.w_pref[nb];
+          seg_next += nb;
+          if (T.prof) pc_win += clock64() - cw0;
         }
-        const uint32_t st = tile % NS;
-        if (tid == 0) {
-          const long long c0 = T.prof ? clock64() : 0;
-          S.pflag = wait_or_abort(&S.sfree[st], ((tile / NS) & 1) ^ 1, abort_flag, T.wait_limit) ? 1u : 0u;
-          if (T.prof) pw_sfree += clock64() - c0;
-        }
-        prod_sync();
-        if (!S.pflag) {
-          aborted = true;
-          break;
-        }
-        const uint32_t wpos = S.w_pos, wtot = S.w_total;
-        const uint32_t ncols = min((uint32_t)TN, wtot - wpos);
-        const bool last = (wpos + TN >= wtot) && (S.seg_next >= U.s1);
-        // candidate position of column tid
+        const uint32_t ncols = min((uint32_t)TN, w_total - w_pos);
+        const bool last = (w_pos + TN >= w_total) && (seg_next >= U.s1);
         uint32_t q = 0xffffffffu;
-        if ((uint32_t)tid < ncols) {
-          const uint32_t rank = wpos + tid;
-          int lo = 0, hi = (int)S.w_nb - 1;
+        if (half == 0 && prow < ncols) {
+          const uint32_t rank = w_pos + prow;
+          int lo = 0, hi = (int)w_nb - 1;
           while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
             if (S.w_pref[mid] <= rank) lo = mid; else hi = mid - 1;
           }
           q = S.w_start[lo] + (rank - S.w_pref[lo]);
         }
-        S.qpos[st][tid] = q;
-        S.qid[st][tid] = (uint32_t)tid < ncols ? P.ids[q] : 0u;
-#pragma unroll
-        for (int g = 0; g < G; ++g) S.aid[st][g * TM + tid] = my_aid[g];
+        q = __shfl_sync(FULL_MASK, q, lane & 15);
+        __nv_bfloat16 *dh, *dl;  // landing slot of the raw rows
+        uint32_t* iddst;  // candidate ids
+        if (RAW > 0) {
+          // own-row slots, last read by this thread when it converted tile
+          // issued - RAW: no wait needed
+          const uint32_t rs = issued % (RAW > 0 ? RAW : 1);
+          dh = Raw + rs * 2 * OPB;
+          dl = dh + OPB;
+          iddst = S.rid[rs];
+        } else {
+          const uint32_t st = issued % NS;
+          const uint32_t sl = pf++ & 1;
+          if (tid == 0) {
+            const long long c0 = T.prof ? clock64() : 0;
+            S.pflag[sl] = wait_or_abort(&S.sfree[st], ((issued / NS) & 1) ^ 1, abort_flag, T.wait_limit) ? 1u : 0u;
+            if (T.prof) pw_sfree += clock64() - c0;
+          }
+          prod_sync();
+          if (!S.pflag[sl]) return 2;
+          dh = Bhi + st * OPB;
+          dl = Blo + st * OPB;
+          iddst = S.qid[st];
+        }
+        if (prow < ncols) {
+          if (half == 0)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(&iddst[prow])), "l"(P.ids + q)
+                         : "memory");
+          load_half<KP>(dh, dl, prow, half, X + (size_t)q * P.dpad, P.dpad);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        pq |= (ncols | (last ? 0x100u : 0u)) << (9 * (issued - tile));  // uniform queue of (columns, last)
+        if (tid == 0) {
+          uint32_t hcr = 0, hq = 0;
+          if (w_hj >= 0) {
+            const uint32_t hr0 = S.w_pref[w_hj], hr1 = S.w_pref[w_hj + 1];
+            const uint32_t lo = max(hr0, w_pos) - w_pos, hi = min(hr1, w_pos + ncols) - w_pos;
+            if (max(hr0, w_pos) < min(hr1, w_pos + ncols)) {
+              hcr = lo | (hi << 8);
+              hq = hs + (w_pos + lo - hr0);
+            }
+          }
+          S.hx[issued & 3][0] = hcr;
+          S.hx[issued & 3][1] = hq;
+        }
+        w_pos += TN;
+        ++issued;
+        return 1;
+      };
+
+      bool first = true, aborted = false;
+      for (;;) {
+        while (issued < tile + LA && (w_pos < w_total || seg_next < U.s1)) {
+          if (advance() == 2) {
+            aborted = true;
+            break;
+          }
+        }
+        if (aborted || issued == tile) break;
+        const long long cc0 = T.prof ? clock64() : 0;
+        switch (issued - tile - 1) {  // groups newer than this tile's
+          case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
+          case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
+          default: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
+        }
+        if (T.prof) pc_ldw += clock64() - cc0;
+        const uint32_t st = tile % NS;
+        const uint32_t ncols = pq & 0xffu;
+        const bool last = (pq & 0x100u) != 0u;
+        pq >>= 9;
         __nv_bfloat16* bh = Bhi + st * OPB;
         __nv_bfloat16* bl = Blo + st * OPB;
-        if ((uint32_t)tid < ncols) {
-          const float* xr = X + (size_t)q * P.dpad;
-          // norm first (the threshold depends on it), then the row
-          const float nq2 = row_norm(xr, S.center, P.d, P.dpad);
-          float tcol, dl;
-          if (!column_threshold(T, ra2max, nq2, &tcol, &dl)) {
-            tcol = 1e30f;    // every row of this column becomes a candidate ...
-            dl = INFINITY;   // ... and none is accepted without the FP64 check
+        const __nv_bfloat16* sh = bh;  // raw rows: in place, or in the landing slot
+        const __nv_bfloat16* sl = bl;
+        if (RAW > 0) {
+          const uint32_t rs = tile % (RAW > 0 ? RAW : 1);
+          const uint32_t id = S.rid[rs][prow];  // own row's id (half 0 copied it)
+          sh = Raw + rs * 2 * OPB;
+          sl = sh + OPB;
+          const uint32_t fl = pf++ & 1;
+          if (tid == 0) {
+            const long long c0 = T.prof ? clock64() : 0;
+            S.pflag[fl] = wait_or_abort(&S.sfree[st], ((tile / NS) & 1) ^ 1, abort_flag, T.wait_limit) ? 1u : 0u;
+            if (T.prof) pw_sfree += clock64() - c0;
           }
-          write_row2<KP>(bh, bl, tid, xr, S.center, P.d, P.dpad, false, nq2, tcol);
-          S.dlt[st][tid] = dl;
-        } else {
-          zero_row2<KP>(bh, bl, tid);
-          S.dlt[st][tid] = 0.f;
+          prod_sync();
+          if (!S.pflag[fl]) {
+            aborted = true;
+            break;
+          }
+          if (half == 0) S.qid[st][prow] = id;
         }
+        const bool ok = prow < ncols;
+        const float part = conv_pass1<KP>(sh, sl, bh, bl, prow, half, ok, S.cadd_b, -2.f, P.d);
+        const float nq2 = (part + __shfl_xor_sync(FULL_MASK, part, 16)) * 0.25f;
+        float tcol = 0.f, dl = 0.f;
+        if (ok && !column_threshold(T, ra2max, nq2, &tcol, &dl)) {
+          tcol = 1e30f;   // every row of this column becomes a candidate ...
+          dl = INFINITY;  // ... and none is accepted without the FP64 check
+        }
+        conv_pass2<KP>(sh, sl, bh, bl, prow, half, ok, S.cadd_b, -2.f, P.d, 1.f, nq2 - tcol);
+        if (half == 0) S.dlt[st][prow] = dl;
+#pragma unroll
+        for (int i = 0; i < (G + 1) / 2; ++i)
+          if (2 * i + (int)half < G) S.aid[st][(2 * i + half) * TM + prow] = my_aid[i];
         if (tid == 0) {
-          S.meta[st] = TileMeta{a0, na, hs, he, ncols, (first ? FLAG_FIRST : 0u) | (last ? FLAG_LAST : 0u), ng};
+          S.meta[st] = TileMeta{a0, na, ncols, (first ? FLAG_FIRST : 0u) | (last ? FLAG_LAST : 0u), ng,
+                                S.hx[tile & 3][0], S.hx[tile & 3][1]};
           n_tiles += 1;
           n_cells += (unsigned long long)na * ncols;
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive(&S.full[st]);
+        if (T.prof) pc_conv += clock64() - cc0;
         first = false;
         ++tile;
-        prod_sync();
-        if (tid == 0) S.w_pos = wpos + TN;
-        prod_sync();
       }
+      asm volatile("cp.async.wait_all;" ::: "memory");
       ++unit_k;
       if (aborted) {
         end_marker();
@@ -525,8 +639,12 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
     if (tid == 0 && T.prof) {
       atomicAdd(&T.ctr->prof[0], (unsigned long long)pw_sfree);
       atomicAdd(&T.ctr->prof[1], (unsigned long long)(clock64() - p_start));
+      atomicAdd(&T.ctr->prof[7], (unsigned long long)pc_unit);
+      atomicAdd(&T.ctr->prof[8], (unsigned long long)pc_win);
+      atomicAdd(&T.ctr->prof[9], (unsigned long long)pc_conv);
+      atomicAdd(&T.ctr->prof[14], (unsigned long long)pc_ldw);
     }
-  } else if (warp == 8) {
+  } else if (warp == MMA_WARP) {
     // ============================ MMA issuer
     // B tiles come in stage order; each is multiplied with the unit's ng home
     // chunks into alternating TMEM accumulators (MMA tile counter mt).
@@ -544,26 +662,26 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
         const bool fok = wait_or_abort(&S.full[st], (tile / NS) & 1, abort_flag, T.wait_limit);
         if (T.prof) mw_full += clock64() - c0;
         if (!fok) {
-          mbar_arrive(&S.dfull[mt & 1]);
+          mbar_arrive(&S.dfull[mt % NACC]);
           break;
         }
         const uint32_t flags = S.meta[st].flags;
         const uint32_t ng = S.meta[st].ng;
         if (flags & FLAG_END) {
-          mbar_arrive(&S.dfull[mt & 1]);
+          mbar_arrive(&S.dfull[mt % NACC]);
           break;
         }
         bool ok = true;
         if (flags & FLAG_FIRST) ok = wait_or_abort(&S.afull, unit_k & 1, abort_flag, T.wait_limit);
         if (!ok) {
-          mbar_arrive(&S.dfull[mt & 1]);
+          mbar_arrive(&S.dfull[mt % NACC]);
           break;
         }
         const uint32_t bh = smem_u32(Bhi + st * OPB), bl = smem_u32(Blo + st * OPB);
         for (uint32_t g = 0; g < ng && ok; ++g) {
-          const uint32_t b = mt & 1;
+          const uint32_t b = mt % NACC;
           const long long c1 = T.prof ? clock64() : 0;
-          ok = wait_or_abort(&S.dfree[b], ((mt >> 1) & 1) ^ 1, abort_flag, T.wait_limit);
+          ok = wait_or_abort(&S.dfree[b], ((mt / NACC) & 1) ^ 1, abort_flag, T.wait_limit);
           if (T.prof) mw_dfree += clock64() - c1;
           if (!ok) {
             mbar_arrive(&S.dfull[b]);
@@ -585,7 +703,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
           }
           tc_commit(&S.dfull[b]);
           last_b = (int)b;
-          last_par = (mt >> 1) & 1;
+          last_par = (mt / NACC) & 1;
           ++mt;
         }
         if (!ok) break;
@@ -599,6 +717,7 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
         atomicAdd(&T.ctr->prof[2], (unsigned long long)mw_full);
         atomicAdd(&T.ctr->prof[3], (unsigned long long)mw_dfree);
         atomicAdd(&T.ctr->prof[4], (unsigned long long)(clock64() - m_start));
+        atomicAdd(&T.ctr->prof[12], (unsigned long long)mt);
       }
       // an aborting CTA may still have MMAs in flight: wait (bounded) for the
       // last committed tile, MMAs complete in issue order
@@ -608,21 +727,24 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
       }
     }
     __syncwarp();
-  } else {
-    // ============================ epilogue (warps 4-7)
-    const uint32_t quarter = warp - 4;
-    float* my_sv = sv + (size_t)(quarter * 32 + lane) * SV_STRIDE;
-    PairStage ps{reinterpret_cast<unsigned long long*>(sv + (size_t)4 * 32 * SV_STRIDE) + quarter * PSTAGE, 0};
-    uint32_t band_cnt = 0, amb_cnt = 0;
+  } else if (warp >= EPI0 && warp < EPI0 + NEPI) {
+    // ============================ epilogue (NEPI warps)
+    // warp w reads TMEM lane quarter w % 4 (the hardware's access rule) and
+    // the 32-column blocks (w - EPI0) / 4, + NEPI / 4, ... of each 128 x 128
+    // accumulator
+    const uint32_t quarter = warp & 3;
+    const uint32_t cblk0 = (warp - EPI0) >> 2;
+    PairStage ps{pstage + (warp - EPI0) * PSTAGE, 0};
+    PairStage bs{pstage + (NEPI + warp - EPI0) * PSTAGE, 0};
     uint32_t tile = 0, mt = 0, g = 0;
-    long long ew_dfull = 0;
+    long long ew_dfull = 0, ec_ld = 0, ec_slow = 0, ec_stage = 0;
     const long long e_start = T.prof ? clock64() : 0;
     for (;;) {
-      const uint32_t st = tile % NS, b = mt & 1;
+      const uint32_t st = tile % NS, b = mt % NACC;
       // all lanes wait; the outcome is made warp-uniform (tcgen05.ld is .sync.aligned)
-      const long long c0 = T.prof ? clock64() : 0;
-      const bool ok = __all_sync(FULL_MASK, wait_or_abort(&S.dfull[b], (mt >> 1) & 1, abort_flag, T.wait_limit));
-      if (T.prof) ew_dfull += clock64() - c0;
+      const long long cw = T.prof ? clock64() : 0;
+      const bool ok = __all_sync(FULL_MASK, wait_or_abort(&S.dfull[b], (mt / NACC) & 1, abort_flag, T.wait_limit));
+      if (T.prof) ew_dfull += clock64() - cw;
       if (!ok) break;
       const TileMeta M = S.meta[st];
       if (__any_sync(FULL_MASK, (M.flags & FLAG_END) || *abort_flag)) break;
@@ -630,47 +752,65 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
       const uint32_t row = g * TM + quarter * 32 + lane;  // row within the unit
       const bool row_ok = row < M.na;
       const uint32_t a_sorted = M.a0 + row;
-      // a quarter whose 32 rows all lie past the home chunk has nothing to do;
-      // TMEM is read two 32-column chunks at a time (both loads in flight)
-      auto process_chunk = [&](const uint32_t (&v)[32], uint32_t c0) {
+#pragma unroll 1
+      for (uint32_t c0 = 32 * cblk0; c0 < TN; c0 += 32 * (NEPI / 4)) {
+      if (g * TM + quarter * 32 < M.na && c0 < M.ncols) {
+        uint32_t v[32];
+        const long long cl0 = T.prof ? clock64() : 0;
+        tmem_ld32_nowait(tbase + b * TN + ((quarter * 32u) << 16) + c0, v);
+        tmem_wait();
+        if (T.prof) ec_ld += clock64() - cl0;
         uint32_t o = 0;
 #pragma unroll
         for (int j = 0; j < 32; ++j) o |= v[j];
-        uint32_t acc_bits = 0;
-        const uint32_t nvalid = M.ncols > c0 ? min(32u, M.ncols - c0) : 0u;
-        const bool maybe = row_ok && nvalid && (o >> 31);
+        uint32_t acc_bits = 0, band_bits = 0;
+        const uint32_t nvalid = min(32u, M.ncols - c0);
+        const bool maybe = row_ok && (o >> 31);
+        const long long cs0 = T.prof ? clock64() : 0;
         if (__any_sync(FULL_MASK, maybe)) {
           if (maybe) {
             uint32_t m = 0;
 #pragma unroll
             for (int j = 0; j < 32; ++j) m |= (v[j] >> 31) << j;
             m &= nvalid >= 32 ? FULL_MASK : ((1u << nvalid) - 1u);
-#pragma unroll
-            for (int j = 0; j < 32; j += 4)
-              *reinterpret_cast<float4*>(my_sv + j) =
-                  make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]), __uint_as_float(v[j + 2]),
-                              __uint_as_float(v[j + 3]));
+            // home bin: a pair (a, q) of two home rows is kept only for a < q
+            // (sorted positions); the home rows of this tile are the columns
+            // [hlo, hhi), column c at position hq + c - hlo
+            const uint32_t hlo = M.hcr & 255u, hhi = M.hcr >> 8;
+            if (hlo < hhi && a_sorted >= M.hq) {
+              const uint32_t lim = hlo + min(a_sorted - M.hq, 255u) + 1;  // columns < lim have q <= a
+              const int e0 = (int)max(hlo, c0) - (int)c0, e1 = (int)min(min(hhi, lim), c0 + 32) - (int)c0;
+              if (e0 < e1) m &= ~((e1 >= 32 ? FULL_MASK : ((1u << e1) - 1u)) & ~((1u << e0) - 1u));
+            }
             while (m) {
               const int j = __ffs(m) - 1;
               m &= m - 1;
-              const uint32_t q = S.qpos[st][c0 + j];
-              if (q >= M.hs && q < M.he && q <= a_sorted) continue;  // home bin: only a < q
-              if (my_sv[j] <= -S.dlt[st][c0 + j]) {
+              // v[j] without dynamic register indexing: a 5-level select tree
+              uint32_t t16[16], t8[8], t4[4], t2[2];
+#pragma unroll
+              for (int k = 0; k < 16; ++k) t16[k] = (j & 16) ? v[16 + k] : v[k];
+#pragma unroll
+              for (int k = 0; k < 8; ++k) t8[k] = (j & 8) ? t16[8 + k] : t16[k];
+#pragma unroll
+              for (int k = 0; k < 4; ++k) t4[k] = (j & 4) ? t8[4 + k] : t8[k];
+#pragma unroll
+              for (int k = 0; k < 2; ++k) t2[k] = (j & 2) ? t4[2 + k] : t4[k];
+              const float vj = __uint_as_float((j & 1) ? t2[1] : t2[0]);
+              if (vj <= -S.dlt[st][c0 + j])
                 acc_bits |= 1u << j;
-              } else {
-                const double sd = exact_sqdist_tc(P, S.aid[st][row], S.qid[st][c0 + j]);
-                ++band_cnt;
-                if (fabs(sd - P.eps2) <= P.amb) ++amb_cnt;
-                if (sd <= P.eps2) acc_bits |= 1u << j;
-              }
+              else
+                band_bits |= 1u << j;  // decided later in FP64 (band list)
             }
           }
         }
-        {
-          const uint32_t ia = acc_bits ? S.aid[st][row] : 0u;
-          uint32_t bits = acc_bits;
+        __syncwarp();
+        const long long cs1 = T.prof ? clock64() : 0;
+        if (T.prof) ec_slow += cs1 - cs0;
+        const uint32_t ia = (acc_bits | band_bits) ? S.aid[st][row] : 0u;
+        auto emit = [&](PairStage& stg, uint32_t bits, unsigned long long* counter, unsigned long long* list,
+                        unsigned long long lcap) {
           stage_pairs(
-              ps, __popc(acc_bits),
+              stg, __popc(bits),
               [&](uint32_t) {
                 const int j = __ffs(bits) - 1;
                 bits &= bits - 1;
@@ -678,19 +818,12 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
                 const uint32_t lo = ia < iq ? ia : iq, hi = ia < iq ? iq : ia;
                 return ((unsigned long long)lo << 32) | hi;
               },
-              &P.ctr->pairs, P.pairs, P.cap);
-        }
-            };
-      if (g * TM + quarter * 32 < M.na) {
-        for (uint32_t c0 = 0; c0 < M.ncols; c0 += 64) {
-          uint32_t v0[32], v1[32];
-          const uint32_t ta = tbase + b * TN + ((quarter * 32u) << 16) + c0;
-          tmem_ld32_nowait(ta, v0);
-          tmem_ld32_nowait(ta + 32, v1);
-          tmem_wait();
-          process_chunk(v0, c0);
-          if (c0 + 32 < M.ncols) process_chunk(v1, c0 + 32);
-        }
+              counter, list, lcap);
+        };
+        if (__any_sync(FULL_MASK, acc_bits != 0u)) emit(ps, acc_bits, &P.ctr->pairs, P.pairs, P.cap);
+        if (__any_sync(FULL_MASK, band_bits != 0u)) emit(bs, band_bits, &P.ctr->band_n, P.band_list, P.band_cap);
+        if (T.prof) ec_stage += clock64() - cs1;
+      }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
@@ -708,45 +841,50 @@ __global__ void __launch_bounds__(TC_THREADS2, 2) k_join_tc(const JoinParams P, 
       }
     }
     stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
+    stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap);
     if (T.prof && lane == 0) {
       atomicAdd(&T.ctr->prof[5], (unsigned long long)ew_dfull);
       atomicAdd(&T.ctr->prof[6], (unsigned long long)(clock64() - e_start));
-    }
-    const uint32_t bt = __shfl_sync(FULL_MASK, warp_scan_incl(band_cnt), 31);
-    const uint32_t at = __shfl_sync(FULL_MASK, warp_scan_incl(amb_cnt), 31);
-    if (lane == 0) {
-      if (bt) atomicAdd(&P.ctr->band, (unsigned long long)bt);
-      if (at) atomicAdd(&P.ctr->ambiguous, (unsigned long long)at);
+      atomicAdd(&T.ctr->prof[10], (unsigned long long)ec_ld);
+      atomicAdd(&T.ctr->prof[11], (unsigned long long)ec_slow);
+      atomicAdd(&T.ctr->prof[13], (unsigned long long)ec_stage);
     }
   }
   // all roles meet here before tensor memory is released
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (warp == 8) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tbase));
+  if (warp == MMA_WARP) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
   if (tid == 0 && S.abort_flag) atomicExch(&P.ctr->error, 1ull);
 }
 
+// Stages and home chunks per KP within about 200 KB of operands: one CTA per
+// SM (512 TMEM columns).
+template <int KP>
+struct TcShape {
+  static constexpr int G = KP <= 32 ? 4 : (KP <= 64 ? 2 : 1);
+  static constexpr int NS = KP <= 32 ? 4 : (KP <= 96 ? 3 : 2);
+  static constexpr int RAW = KP <= 48 ? 3 : 0;  // separate landing slots where they fit
+  // short rows: many tiles, pairs and hits per converted row -> more epilogue
+  // warps (16: 72 registers a thread); long rows: 8 (96 registers)
+  static constexpr int NEPI = KP <= 48 ? 16 : 8;
+};
+
 template <int KP>
 void launch_tc(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
-  constexpr int NS = KP <= 64 ? 3 : 2;
-  constexpr int G = KP <= 32 ? 2 : 1;  // home chunks per unit (must match tc_rows)
-  const size_t dyn = (2 * G + 2 * NS) * (size_t)TM * KP * sizeof(__nv_bfloat16) +
-                     (size_t)4 * 32 * SV_STRIDE * sizeof(float) + 4 * PSTAGE * sizeof(unsigned long long);
-  MCK(cudaFuncSetAttribute(k_join_tc<KP, NS, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-  MCK(cudaFuncSetAttribute(k_join_tc<KP, NS, G>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  constexpr int NS = TcShape<KP>::NS, G = TcShape<KP>::G, RAW = TcShape<KP>::RAW, NEPI = TcShape<KP>::NEPI;
+  constexpr int NT = tc_threads(NEPI);
+  const size_t dyn = (2 * G + 2 * NS + 2 * RAW) * (size_t)TM * KP * sizeof(__nv_bfloat16) +
+                     (size_t)2 * NEPI * PSTAGE * sizeof(unsigned long long);
+  MCK(cudaFuncSetAttribute(k_join_tc<KP, NS, G, RAW, NEPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  MCK(cudaFuncSetAttribute(k_join_tc<KP, NS, G, RAW, NEPI>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
-  MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join_tc<KP, NS, G>, TC_THREADS2, dyn));
+  MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join_tc<KP, NS, G, RAW, NEPI>, NT, dyn));
   if (per_sm < 1) throw Error(MISTIC_ERR_TOO_LARGE, "tensor-core join does not fit on an SM");
-  const int occ = per_sm;
-  // two CTAs per SM: 256 TMEM columns each (512 per SM), and registers and
-  // shared memory allow two for every KP <= 64; the occupancy query reports
-  // one for this 9-warp block, so it only serves as the fits-at-all check
-  per_sm = (dyn + sizeof(TcShared2<NS, G>) + 1024) * 2 <= 228 * 1024 ? 2 : 1;
-  const unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)per_sm * h->sms, T.n_units);
+  const unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)h->sms, T.n_units);
   if (getenv("MISTIC_DEBUG"))
-    fprintf(stderr, "[mistic] join_tc KP=%d NS=%d dyn=%zu occupancy=%d grid=%u units=%llu\n", KP, NS, dyn, occ, grid,
-            (unsigned long long)T.n_units);
-  k_join_tc<KP, NS, G><<<grid, TC_THREADS2, dyn, h->stream>>>(P, T);
+    fprintf(stderr, "[mistic] join_tc KP=%d NS=%d G=%d RAW=%d NEPI=%d dyn=%zu occupancy=%d grid=%u units=%llu\n", KP,
+            NS, G, RAW, NEPI, dyn, per_sm, grid, (unsigned long long)T.n_units);
+  k_join_tc<KP, NS, G, RAW, NEPI><<<grid, NT, dyn, h->stream>>>(P, T);
   launched(h, "join_tc");
 }
 
@@ -757,7 +895,10 @@ namespace join {
 int tc_kp(uint32_t d) { return (int)(((d + 2) + 15) / 16 * 16); }
 // Home rows per tensor-core unit: G chunks of 128 share each converted
 // candidate tile (G = 2 while the operands leave room for two CTAs per SM).
-uint32_t tc_rows(uint32_t d) { return tc_kp(d) <= 32 ? 2 * TM : TM; }
+uint32_t tc_rows(uint32_t d) {
+  const int kp = tc_kp(d);
+  return (uint32_t)TM * (kp <= 32 ? 4 : (kp <= 64 ? 2 : 1));
+}
 bool tc_supported(uint32_t d) { return tc_kp(d) <= 128; }
 
 void run_tc(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {

@@ -501,16 +501,32 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   jp.pairs = pbuf;
   jp.cap = cap;
   jp.ctr = ctr;
+  // band list: pairs the FP32 / tensor-core joins leave to the FP64 check
+  if (!fp64) {
+    unsigned long long bcap = std::max<unsigned long long>(1ull << 20, 2ull * n);
+    auto it = h->arena.bufs.find("band");
+    if (it != h->arena.bufs.end()) bcap = std::max<unsigned long long>(bcap, it->second.bytes / 8);
+    // MISTIC_BAND_CAP=k starts from a k-entry list (tests of the overflow path)
+    if (const char* e = getenv("MISTIC_BAND_CAP")) bcap = std::max<unsigned long long>(1, strtoull(e, nullptr, 10));
+    jp.band_list = abuf<unsigned long long>(h, "band", bcap);
+    jp.band_cap = bcap;
+  }
   JoinCounters hc{};
-  for (int attempt = 0; attempt < 2; ++attempt) {
+  for (int attempt = 0; attempt < 3; ++attempt) {
     MCK(cudaMemsetAsync(ctr, 0, 2 * sizeof(JoinCounters), h->stream));
     if (o.timing) MCK(cudaEventRecord(h->jev[0], h->stream));
     join::run(h, fp64, CH, jp);
     if (o.timing) MCK(cudaEventRecord(h->jev[1], h->stream));
     if (use_tc) join::run_tc(h, jp, tp);
     if (o.timing) MCK(cudaEventRecord(h->jev[2], h->stream));
+    join::run_band(h, jp);
     d2h(h, &hc, ctr, sizeof hc);
     if (hc.error) throw Error(MISTIC_ERR_TIMEOUT, "a tensor-core tile wait timed out");
+    if (hc.band_n > jp.band_cap) {  // band list overflowed: nothing beyond it was decided, run again
+      jp.band_cap = hc.band_n + hc.band_n / 4;
+      jp.band_list = abuf<unsigned long long>(h, "band", jp.band_cap);
+      continue;
+    }
     if (!need_pairs || hc.pairs <= cap || o.pair_capacity) break;
     cap = hc.pairs;
     pbuf = abuf<unsigned long long>(h, "pairs", cap);
@@ -534,6 +550,14 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
               "%.1f%% | epilogue wait-acc %.1f%%\n",
               tot_p ? 100.0 * tcc.prof[0] / tot_p : 0.0, tot_m ? 100.0 * tcc.prof[2] / tot_m : 0.0,
               tot_m ? 100.0 * tcc.prof[3] / tot_m : 0.0, tot_e ? 100.0 * tcc.prof[5] / tot_e : 0.0);
+      fprintf(stderr,
+              "[mistic] join_tc detail: producers unit %.1f%% window %.1f%% convert %.1f%% (rows-wait %.1f%%) | epilogue tmem-ld "
+              "%.1f%% slow %.1f%% stage %.1f%% | %llu tiles, %llu accumulator tiles\n",
+              tot_p ? 100.0 * tcc.prof[7] / tot_p : 0.0, tot_p ? 100.0 * tcc.prof[8] / tot_p : 0.0,
+              tot_p ? 100.0 * tcc.prof[9] / tot_p : 0.0, tot_p ? 100.0 * tcc.prof[14] / tot_p : 0.0,
+              tot_e ? 100.0 * tcc.prof[10] / tot_e : 0.0,
+              tot_e ? 100.0 * tcc.prof[11] / tot_e : 0.0, tot_e ? 100.0 * tcc.prof[13] / tot_e : 0.0,
+              (unsigned long long)tcc.tiles, (unsigned long long)tcc.prof[12]);
     }
   }
 

@@ -100,6 +100,20 @@ def test_modes_agree_and_band_is_small(handle):
     assert a.band_pairs < 0.01 * a.candidates + 1000
 
 
+@pytest.mark.parametrize("mode", ["fp32", "bf16"])
+def test_band_list_overflow_reruns(handle, monkeypatch, mode):
+    """A band list far too short for the band pairs: the join runs again with
+    a longer list and the pair set stays exact."""
+    from mistic import workloads as W
+    x = W.gen_susy_like(30000, seed=9)
+    eps = 0.03
+    ref = O.brute_pairs(x, eps)
+    monkeypatch.setenv("MISTIC_BAND_CAP", "2")
+    r = run(handle, x, 6, eps, mode=mode)
+    assert r.band_pairs > 2
+    assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)
+
+
 def test_f32_input_uses_widened_predicate(handle):
     x = np.random.default_rng(8).normal(size=(4000, 33)).astype(np.float32)
     eps = 5.0
