@@ -84,7 +84,8 @@ typedef enum mistic_rp_mode {
 
 typedef enum mistic_pairs_where {
   MISTIC_PAIRS_NONE = 0,   /* counts only; no pair list is materialised */
-  MISTIC_PAIRS_HOST = 1,   /* result.pairs is a host array owned by the result */
+  MISTIC_PAIRS_HOST = 1,   /* result.pairs is a host array owned by the result (pinned memory
+                              from a process-wide cache: release it with mistic_result_free) */
   MISTIC_PAIRS_DEVICE = 2  /* result.pairs is a device array owned by the result */
 } mistic_pairs_where;
 

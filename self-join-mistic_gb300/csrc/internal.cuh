@@ -138,7 +138,7 @@ struct TcParams {
   float Dp;                // 1.1 sqrt(eps2)
   float cap;               // 0.1 eps2: larger bounds re-decide the whole column in FP64
   float margin;            // small positive slack that makes D' >= 0 a strict reject
-  long long wait_limit;    // try_wait iterations before a barrier wait gives up
+  long long wait_limit;    // nanoseconds before a barrier wait gives up
   int stall_test;          // failure-detection test: the MMA warp never signals (waits run out)
   int prof;                // record per-role wait/total cycles into ctr->prof (diagnostics)
 };

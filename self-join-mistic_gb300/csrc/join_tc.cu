@@ -51,7 +51,6 @@ namespace {
 constexpr int TM = 128;          // home rows per tile (MMA M)
 constexpr int TN = 128;          // candidate columns per tile (MMA N)
 constexpr int WIN = 256;         // neighbour bins per candidate window
-constexpr long long kWaitLimit = 1ll << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -168,21 +167,41 @@ __device__ __forceinline__ void tc_commit(unsigned long long* b) {
 }
 __device__ __forceinline__ void prod_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NPROD) : "memory"); }
 
-// Bounded wait; on expiry raise the CTA's abort flag.  Returns false if the
-// CTA is aborting (now or already).
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait on an mbarrier phase.  The waiting warp is suspended by the
+// hardware (try_wait with a suspend-time hint) instead of spinning, so idle
+// roles leave the issue slots to the working ones.  After limit_ns of
+// waiting the CTA's abort flag is raised.  Returns false if the CTA is
+// aborting (now or already).
+constexpr uint32_t kSuspendNs = 20000;
 __device__ __forceinline__ bool wait_or_abort(unsigned long long* b, uint32_t parity, volatile uint32_t* abort_flag,
-                                              long long limit = kWaitLimit) {
+                                              long long limit_ns) {
   const uint32_t a = smem_u32(b);
-  for (long long it = 0; it < limit; ++it) {
-    uint32_t done;
-    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-                 : "=r"(done)
-                 : "r"(a), "r"(parity));
+  uint32_t done;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(done)
+               : "r"(a), "r"(parity)
+               : "memory");
+  if (done) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity), "r"(kSuspendNs)
+        : "memory");
     if (done) return true;
-    if ((it & 255) == 255 && *abort_flag) return false;
+    if (*abort_flag) return false;
+    if ((long long)(global_ns() - t0) > limit_ns) {
+      *abort_flag = 1u;
+      return false;
+    }
   }
-  *abort_flag = 1u;
-  return false;
 }
 
 // Operand rows live in the no-swizzle K-major core-matrix layout: the

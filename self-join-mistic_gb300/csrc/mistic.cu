@@ -23,6 +23,9 @@
 #include <cmath>
 #include <cstdio>
 #include <fstream>
+#include <map>
+#include <mutex>
+#include <unordered_map>
 #include <vector>
 
 #include "internal.cuh"
@@ -117,6 +120,72 @@ bool filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_
 
 namespace {
 
+// Process-wide cache of pinned host blocks for result arrays: a device-to-
+// host copy into pinned memory runs at the link's speed, one into fresh
+// pageable memory stalls on page faults.  Blocks come in size classes of at
+// most 12.5% waste, are handed to a result and come back here from
+// mistic_result_free; up to kMaxCached bytes stay cached for the next call.
+class PinnedCache {
+ public:
+  void* acquire(size_t bytes) {
+    const size_t cls = size_class(bytes);
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      auto it = free_.lower_bound(cls);
+      if (it != free_.end() && it->first <= 2 * cls) {
+        void* p = it->second;
+        cached_ -= it->first;
+        free_.erase(it);
+        return p;
+      }
+    }
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, cls, cudaHostAllocPortable) != cudaSuccess) {
+      cudaGetLastError();  // clear; the caller falls back to pageable memory
+      return nullptr;
+    }
+    std::lock_guard<std::mutex> g(mu_);
+    size_[p] = cls;
+    return p;
+  }
+  // false: not a block of this cache
+  bool release(void* p) {
+    size_t sz = 0;
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      auto it = size_.find(p);
+      if (it == size_.end()) return false;
+      sz = it->second;
+      if (cached_ + sz <= kMaxCached) {
+        free_.emplace(sz, p);
+        cached_ += sz;
+        return true;
+      }
+      size_.erase(it);
+    }
+    cudaFreeHost(p);
+    return true;
+  }
+
+ private:
+  static constexpr size_t kMaxCached = 8ull << 30;
+  static size_t size_class(size_t bytes) {
+    if (bytes <= (1u << 16)) return 1u << 16;
+    int lg = 63 - __builtin_clzll((unsigned long long)bytes);
+    const size_t step = (size_t)1 << (lg - 3);
+    return (bytes + step - 1) / step * step;
+  }
+  std::mutex mu_;
+  std::multimap<size_t, void*> free_;
+  std::unordered_map<void*, size_t> size_;
+  size_t cached_ = 0;
+};
+
+PinnedCache& pinned_cache() {
+  static PinnedCache* c = new PinnedCache;  // never destroyed: blocks may outlive static teardown
+  return *c;
+}
+
 template <class T>
 T* abuf(mistic_handle_s* h, const char* name, size_t count) {
   return (T*)h->arena.get(name, count * sizeof(T));
@@ -157,10 +226,15 @@ int bit_length(uint64_t v) {
 
 // Smallest home bin that goes to the tensor-core join.  MISTIC_TC_MIN_BIN
 // overrides it (tuning).
-uint32_t tc_min_bin() {
+// Smallest home bin joined on the tensor cores.  A tensor-core tile costs
+// about the same per candidate row whatever its number of home rows, a
+// CUDA-core unit costs d FMAs per cell, so small bins go to the CUDA cores
+// for short rows only.  Measured on GB300 (5M x 18: best 48-96; 515k x 90:
+// best 1-6): 20000 / d^2, clamped to [1, 64].
+uint32_t tc_min_bin(uint32_t d) {
   const char* e = getenv("MISTIC_TC_MIN_BIN");
   if (e && *e) return (uint32_t)std::max(1l, strtol(e, nullptr, 10));
-  return 16;
+  return (uint32_t)std::min(64.0, std::max(1.0, std::floor(20000.0 / ((double)d * d))));
 }
 
 void check_handle(mistic_handle h) {
@@ -405,7 +479,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   const int CH = join::chunk_for(fp64, fp64 ? dpad64 : dpad32);
   ep.chunk = (uint32_t)CH;
   ep.seg_cap = 4096;
-  ep.tc_min = use_tc ? tc_min_bin() : 0u;
+  ep.tc_min = use_tc ? tc_min_bin(d) : 0u;
   ep.tc_chunk = use_tc ? join::tc_rows(d) : 128;
   uint32_t* nbr_cnt = abuf<uint32_t>(h, "nbr_cnt", m + 1);
   uint32_t* unit_cnt = abuf<uint32_t>(h, "unit_cnt", m + 1);
@@ -478,7 +552,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     // kernel frees its tensor memory and the call returns MISTIC_ERR_TIMEOUT
     const char* st = getenv("MISTIC_TEST_TC_STALL");
     tp.stall_test = (st && *st == '1') ? 1 : 0;
-    tp.wait_limit = tp.stall_test ? (1ll << 12) : (1ll << 22);
+    tp.wait_limit = tp.stall_test ? 2000000ll : 2000000000ll;  // 2 ms in the test, else 2 s
     tp.prof = getenv("MISTIC_DEBUG") ? 1 : 0;
   }
   const bool want_pairs = o.pairs != MISTIC_PAIRS_NONE;
@@ -604,7 +678,8 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     pairs_to_ij(h, pbuf, stored);
     r->pairs_len = stored;
     if (o.pairs == MISTIC_PAIRS_HOST) {
-      uint32_t* hp = (uint32_t*)malloc(std::max<size_t>(1, stored * 8));
+      uint32_t* hp = (uint32_t*)pinned_cache().acquire(std::max<size_t>(1, stored * 8));
+      if (!hp) hp = (uint32_t*)malloc(std::max<size_t>(1, stored * 8));
       if (!hp) throw Error(MISTIC_ERR_OUT_OF_MEMORY, "host pair buffer");
       MCK(cudaMemcpyAsync(hp, pbuf, stored * 8, cudaMemcpyDeviceToHost, h->stream));
       MCK(cudaStreamSynchronize(h->stream));
@@ -842,7 +917,7 @@ void mistic_result_free(mistic_result* r) {
   if (r->pairs && r->_owner) {
     if (r->pairs_on_device)
       cudaFree(r->pairs);
-    else
+    else if (!mistic::pinned_cache().release(r->pairs))
       free(r->pairs);
   }
   r->pairs = nullptr;
