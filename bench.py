@@ -75,6 +75,9 @@ WORKLOADS = {
                   "uniform n=1e5 d=18 FP64, k=6, 32 mean neighbours"),
     "msd90": (_subset(W.msd90, 515_345),
               "MSD-shaped n=515,345 d=90 FP64, k=8, 16 mean neighbours"),
+    # ε calibrated on each generated set (drawn on the GPU at this size)
+    "tiny384": (lambda n: W.tiny384(n or 5_000_000),
+                "TINY-shaped n=5e6 d=384 FP32, 1000 Zipf clusters, L2-normalised, k=8, 16 mean neighbours"),
 }
 
 FALLBACK_PEAKS = {"hbm_gbs": 6785.9, "bf16_tflops": 1922.1, "bf16_tflops_sustained": 1711.2}
@@ -320,7 +323,8 @@ def run_mistic(args, wl) -> None:
         # (d subtractions, d multiply-adds) on the CUDA-core FP32 pipe
         work = r.candidates * 3.0 * d
         achieved = work / (simt_ms * 1e-3) / 1e12
-        roof = {"bound": "fp32", "kernel": "k_join_f32r", "achieved": achieved, "peak": fp32_peak,
+        roof = {"bound": "fp32", "kernel": "k_join_f32r" if d <= 32 else "k_join_f32", "achieved": achieved,
+                "peak": fp32_peak,
                 "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
                 "work": "3*d FP32 flops per candidate pair", "kernel_ms": simt_ms,
                 "peak_source": "mistic_peaks FFMA probe, this run (CUDA-core FP32 pipe)"}
@@ -334,7 +338,7 @@ def run_mistic(args, wl) -> None:
         "config": {"workload": args.workload, "n": n, "d": d, "k": wl.k, "eps_hex": float(wl.eps).hex(),
                    "desc": WORKLOADS[args.workload][1], "mode": r.mode_used,
                    "parallelism": "replicas" if world > 1 else "single",
-                   "l2": f"inputs larger than L2 ({n * d * 8 / 1e6:.0f} MB points per step)",
+                   "l2": f"inputs larger than L2 ({n * d * x.itemsize / 1e6:.0f} MB points per step)",
                    "pairs_to": "caller device buffer"},
         "pairs_ij": r.pairs_ij, "pairs_ordered_incl_self": r.pairs_ordered_incl_self,
         "candidates": r.candidates, "band_pairs": r.band_pairs, "ulp_ambiguous": r.ulp_ambiguous,
@@ -356,6 +360,126 @@ def run_mistic(args, wl) -> None:
             "sample": f"rows [0,{cpu['rows']}) x all {n} rows ({cpu['seconds']:.1f} s), extrapolated to "
                       f"n rows; brute_force of src/utils.cu:285-317 (oracle C port, OpenMP)",
             "evals_per_s": cpu["evals_per_s"]},
+    }
+    print(json.dumps(line), flush=True)
+    h.close()
+
+
+def run_batch(args) -> None:
+    """c4: 2,000 independent instances (n log-uniform in [1e3, 2e5], d in
+    {2,8,18,32,57,90}, FP32 Gaussian mixtures) through one
+    mistic_batch_selfjoin call per step.  value: inputs resident in HBM,
+    counts only; e2e: host inputs and host pair lists.  The batch call is
+    synchronous and spreads instances over worker streams, so a step is timed
+    by the host clock between two device synchronisations."""
+    import torch
+    import mistic
+    from mistic import _lib as L
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    count = args.n or 2000
+    t_gen = time.perf_counter()
+    wls = W.batch_instances_device(count=count, device=f"cuda:{local}")
+    t_gen = time.perf_counter() - t_gen
+    h = mistic.Handle(local)
+    m = len(wls)
+    xs = [np.ascontiguousarray(w.pts) for w in wls]
+    xts = [torch.from_numpy(x).to(dev) for x in xs]
+    torch.cuda.synchronize()
+    inst_h, inst_d = (L.Instance * m)(), (L.Instance * m)()
+    for i, (w, x, xt) in enumerate(zip(wls, xs, xts)):
+        for arr, ptr in ((inst_h, x.ctypes.data), (inst_d, xt.data_ptr())):
+            arr[i].pts, arr[i].n, arr[i].d = ptr, x.shape[0], x.shape[1]
+            arr[i].dtype, arr[i].k, arr[i].eps = L.F32, w.k, float(w.eps)
+    tot_n = sum(x.shape[0] for x in xs)
+
+    def batch(inst, opts):
+        res = (L.Result * m)()
+        st = h.lib.mistic_batch_selfjoin(h.h, inst, m, ctypes.byref(opts), res)
+        mistic._check(h.lib, h.h, st)
+        out = [(int(r.pairs_ij), int(r.kernel_launches), int(r.candidates)) for r in res]
+        for i in range(m):
+            h.lib.mistic_result_free(ctypes.byref(res[i]))
+        return out
+
+    def timed(inst, opts, steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        outs = [batch(inst, opts) for _ in range(steps)]
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3 / steps, outs[-1]
+
+    o_cnt = h.opts(input_on_device=True, mode=args.mode)
+    for _ in range(args.warmup):
+        batch(inst_d, o_cnt)
+    clocks = ClockSampler()
+    clocks.start()
+    ms, res = timed(inst_d, o_cnt, args.steps)
+    clk = clocks.stop()
+    os.environ["MISTIC_BATCH_STREAMS"] = "1"
+    serial_ms, _ = timed(inst_d, o_cnt, 1)
+    del os.environ["MISTIC_BATCH_STREAMS"]
+    o_host = h.opts(pairs="host", mode=args.mode)
+    batch(inst_h, o_host)
+    e2e_ms, _ = timed(inst_h, o_host, args.steps)
+
+    parity = None
+    if not args.no_fp64:
+        f_ms, res64 = timed(inst_d, h.opts(input_on_device=True, mode="fp64"), 1)
+        from oracle import oracle as O
+        small = sorted(range(m), key=lambda i: xs[i].shape[0])[:20]
+        ok = True
+        for i in small:
+            r = h.selfjoin(xs[i], wls[i].k, wls[i].eps, pairs="host", sort_pairs=True, mode=args.mode)
+            ok &= bool(np.array_equal(r.pairs, O.brute_pairs(xs[i], wls[i].eps)))
+        parity = {"fp64_batch_ms": f_ms, "counts_identical_to_fp64": [p[0] for p in res] == [p[0] for p in res64],
+                  "oracle_pair_sets_identical": ok, "oracle_instances": len(small)}
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        # brute force on a row sample of 8 instances; the n^2 d cost model
+        # scales it to the whole batch
+        from oracle import oracle as O
+        threads = O.max_threads()
+        t_s, cost_s = 0.0, 0.0
+        for i in list(range(0, m, max(1, m // 8)))[:8]:
+            x = xs[i]
+            rows = min(x.shape[0], max(64, int(2e8 / max(1, x.shape[0] * x.shape[1]))))
+            t0 = time.perf_counter()
+            O.count_rows(x, wls[i].eps, 0, rows, threads)
+            t_s += time.perf_counter() - t0
+            cost_s += rows * x.shape[0] * x.shape[1]
+        job_s = t_s * sum(x.shape[0] ** 2 * x.shape[1] for x in xs) / cost_s
+        cpu = {"value": tot_n / job_s, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"row samples of 8 instances ({t_s:.1f} s), scaled by sum n^2 d to all {m}; "
+                         "brute_force of src/utils.cu:285-317 (oracle C port, OpenMP)"}
+    pairs = sum(p[0] for p in res)
+    line = {
+        "metric": METRIC, "value": world * tot_n / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "batch2000", "instances": m, "points": tot_n,
+                   "desc": "2,000 instances, n log-uniform [1e3,2e5], d in {2,8,18,32,57,90}, FP32 "
+                           "Gaussian mixtures, 4/16/64 mean neighbours", "mode": args.mode,
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "streams": "worker handles (MISTIC_BATCH_STREAMS default)", "pairs_to": "counts only",
+                   "timing": "host clock around the synchronous batch call, device synchronised",
+                   "l2": f"inputs {sum(x.nbytes for x in xs) / 1e9:.1f} GB in total"},
+        "pairs_ij": pairs, "candidates": sum(p[2] for p in res),
+        "serial_ms_per_step": serial_ms, "stream_speedup": serial_ms / ms,
+        "generation_s": t_gen, "parity": parity,
+        "roofline": None,
+        "e2e": {"value": world * tot_n / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": sum(x.nbytes for x in xs), "d2h_bytes_per_step": pairs * 8},
+        "gpu_launches": sum(p[1] for p in res),
+        "clocks": clk,
+        "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
     h.close()
@@ -384,7 +508,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mistic", "reference"], default="mistic")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="susy18")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch2000"], default="susy18")
     ap.add_argument("--n", type=int, default=0, help="override the point count (testing)")
     ap.add_argument("--mode", choices=["auto", "fp32", "bf16", "fp64"], default="auto",
                     help="join mode of the timed steps")
@@ -393,6 +517,13 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=6.0)
     args = ap.parse_args()
+    if args.workload == "batch2000":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the single-instance "
+                              "workloads; c4 reports its CPU baseline in the mistic line"}), flush=True)
+        else:
+            run_batch(args)
+        return
     wl = WORKLOADS[args.workload][0](args.n)
     if args.impl == "reference":
         run_reference(args, wl)

@@ -191,6 +191,14 @@ mistic_status mistic_read_points(const char* path, uint32_t d, mistic_dtype dtyp
                                  void** out_pts, uint64_t* out_n);
 void mistic_free_host(void* p);
 
+/* Text -> binary converter with the behaviour of the reference's toBin tool
+ * (toCSV.cpp:52-85): reads decimal numbers separated by commas and/or white
+ * space from `text_path`, stopping at the first token that is not a number,
+ * and writes them as raw little-endian FP64 to `bin_path` (the input format
+ * of mistic_read_points and of the reference's main).  *out_count receives
+ * the number of values written (may be NULL).  Host only; needs no GPU. */
+mistic_status mistic_convert_text(const char* text_path, const char* bin_path, uint64_t* out_count);
+
 /* Release the buffers a result owns (pair list).  Safe on a zeroed result. */
 void mistic_result_free(mistic_result* r);
 

@@ -1,7 +1,9 @@
 #!/usr/bin/env bash
 # Builds the reference's own CPU brute-force join (brute_force in
 # src/utils.cu:285-317 of bwd29/self-join-MiSTIC) from its unmodified source
-# where it lies, plus oracle/ref_driver.cpp, into oracle/_ref/ref_brute.
+# where it lies, plus oracle/ref_driver.cpp, into oracle/_ref/ref_brute; and
+# its text -> binary converter (toCSV.cpp, the `toBin` tool) into
+# oracle/_ref/ref_tobin.
 # Only this recipe reads the reference tree; outputs go to oracle/_ref/ only.
 # The reference headers need BS/KB defined (include/params.cuh) and thrust,
 # so the file is compiled with nvcc as host code; no GPU is touched.
@@ -21,3 +23,7 @@ nvcc -O3 -DBS=256 -DKB=1024 -DDIM=18 -I"$REF" -Xcompiler -fopenmp \
 g++ -O2 -fopenmp -c "$HERE/ref_driver.cpp" -o "$OUT/ref_driver.o"
 nvcc -Xcompiler -fopenmp "$OUT/ref_driver.o" "$OUT/ref_utils.o" -o "$OUT/ref_brute"
 echo "built $OUT/ref_brute"
+if [ -f "$REF/toCSV.cpp" ]; then
+  g++ -O2 "$REF/toCSV.cpp" -o "$OUT/ref_tobin"
+  echo "built $OUT/ref_tobin"
+fi

@@ -17,6 +17,11 @@
 //   --seed S
 //   --pairs out.bin    write the i<j pair list as uint32 (i, j) rows, sorted
 //   --device N
+//
+//   mistic --to-bin <in.txt> <out.bin>
+// converts a comma/white-space separated text file into the raw FP64 input
+// format (the reference's toBin tool, toCSV.cpp:52-85) and prints the
+// number of values, as that tool does.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -28,12 +33,23 @@
 static int usage(const char* p) {
   fprintf(stderr,
           "usage: %s <file.bin> <dim> <numRP> <epsilon> [--f32] [--mode auto|fp64|fp32] "
-          "[--rp pca|box] [--seed S] [--pairs out.bin] [--device N]\n",
-          p);
+          "[--rp pca|box] [--seed S] [--pairs out.bin] [--device N]\n"
+          "       %s --to-bin <in.txt> <out.bin>\n",
+          p, p);
   return 2;
 }
 
 int main(int argc, char** argv) {
+  if (argc == 4 && std::string(argv[1]) == "--to-bin") {
+    uint64_t cnt = 0;
+    const mistic_status s = mistic_convert_text(argv[2], argv[3], &cnt);
+    if (s != MISTIC_OK) {
+      fprintf(stderr, "%s\n", mistic_strerror(s));
+      return 1;
+    }
+    printf("size of data: %llu\n", (unsigned long long)cnt);
+    return 0;
+  }
   if (argc < 5) return usage(argv[0]);
   const char* file = argv[1];
   const unsigned dim = (unsigned)strtoul(argv[2], nullptr, 10);

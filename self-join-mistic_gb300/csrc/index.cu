@@ -495,9 +495,9 @@ void rp_dist(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, uint3
   const size_t smem = (size_t)k * d * sizeof(double) + (d <= RPD_DMAX ? (size_t)RPD_THREADS * d * sizeof(double) : 0);
   if (smem > 48 * 1024) {
     if (dt == MISTIC_F64)
-      MCK(cudaFuncSetAttribute(k_rp_dist<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      allow_max_dyn_smem(k_rp_dist<double>);
     else
-      MCK(cudaFuncSetAttribute(k_rp_dist<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      allow_max_dyn_smem(k_rp_dist<float>);
   }
   if (dt == MISTIC_F64)
     k_rp_dist<double><<<nparts, RPD_THREADS, smem, h->stream>>>((const double*)x, n, d, rps, k, D, part);

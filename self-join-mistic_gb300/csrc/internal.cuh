@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -162,6 +163,8 @@ struct mistic_handle_s {
   cudaEvent_t ev[16] = {};
   cudaEvent_t jev[4] = {};  // around the two join kernels
   uint32_t launches = 0;
+  std::vector<mistic_handle_s*> workers;  // batch workers: own streams, same device (created on demand)
+  cudaEvent_t batch_ev = nullptr;         // orders the workers' streams after this handle's stream
 };
 
 namespace mistic {
@@ -169,6 +172,17 @@ namespace mistic {
 // Records a kernel launch for the result's kernel_launches counter and
 // checks the launch status.
 void launched(mistic_handle_s* h, const char* what);
+
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in
+// maximum less the kernel's static shared memory, once per kernel and
+// process.  The limit is a per-function setting; setting it to the size of
+// each launch would let concurrent callers (batch worker threads) lower it
+// under another thread's launch.
+void allow_max_dyn_smem_impl(const void* kern);
+template <class K>
+void allow_max_dyn_smem(K kern) {
+  allow_max_dyn_smem_impl(reinterpret_cast<const void*>(kern));
+}
 
 // ---- scan.cu
 template <class T>

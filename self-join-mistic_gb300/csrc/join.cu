@@ -497,8 +497,7 @@ static void launch_persistent(mistic_handle_s* h, K kern, size_t smem_per_warp, 
   const size_t smem = smem_per_warp * warps;
   if (smem > kBlockSmem + 27 * 1024)
     throw Error(MISTIC_ERR_TOO_LARGE, "join tile does not fit in shared memory for this dimensionality");
-  if (smem > 48 * 1024) MCK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  MCK(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  allow_max_dyn_smem(kern);
   int per_sm = 0;
   MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));
   if (per_sm < 1) throw Error(MISTIC_ERR_TOO_LARGE, "join kernel does not fit on an SM for this dimensionality");

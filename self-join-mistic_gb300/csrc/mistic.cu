@@ -24,7 +24,9 @@
 #include <cstdio>
 #include <fstream>
 #include <map>
+#include <atomic>
 #include <mutex>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -116,6 +118,26 @@ bool filter_thresholds(uint32_t d, double eps2, double R, float* t_lo, float* t_
   *t_lo = flo;
   *t_hi = fhi;
   return true;
+}
+
+void allow_max_dyn_smem_impl(const void* kern) {
+  static std::mutex mu;
+  static std::map<const void*, cudaError_t>* done = new std::map<const void*, cudaError_t>;
+  std::lock_guard<std::mutex> g(mu);
+  auto it = done->find(kern);
+  if (it == done->end()) {
+    cudaError_t err = cudaSuccess;
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa{};
+    if ((err = cudaGetDevice(&dev)) == cudaSuccess &&
+        (err = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) == cudaSuccess &&
+        (err = cudaFuncGetAttributes(&fa, kern)) == cudaSuccess &&
+        (err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    optin - (int)fa.sharedSizeBytes)) == cudaSuccess)
+      err = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    it = done->emplace(kern, err).first;
+  }
+  MCK(it->second);
 }
 
 namespace {
@@ -865,6 +887,8 @@ mistic_status mistic_destroy(mistic_handle h) {
   for (auto& e : h->jev)
     if (e) cudaEventDestroy(e);
   if (h->own_stream) cudaStreamDestroy(h->stream);
+  for (mistic_handle w : h->workers) mistic_destroy(w);
+  if (h->batch_ev) cudaEventDestroy(h->batch_ev);
   delete h;
   return MISTIC_OK;
 }
@@ -874,14 +898,74 @@ mistic_status mistic_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint
   MISTIC_GUARD(h, mistic::run_selfjoin(h, pts, n, d, dtype, k, eps, opts, result));
 }
 
+// Instances run concurrently on a pool of worker handles (own streams, own
+// buffers, created once per handle), driven by host threads that take the
+// next instance from an atomic index: small instances are bound by launch
+// and read-back latency, which the streams overlap.  MISTIC_BATCH_STREAMS
+// sets the pool size (default min(8, host threads); 1 = one after another
+// on this handle).  A caller pair buffer forces the serial order (one
+// buffer cannot hold concurrent lists).  On a failure the lowest failing
+// instance's status and message are returned; instances not run keep a
+// zeroed result.
 mistic_status mistic_batch_selfjoin(mistic_handle h, const mistic_instance* inst, uint32_t m,
                                     const mistic_opts* opts, mistic_result* results) {
   if (!h || (m > 0 && (!inst || !results))) return fail(h, MISTIC_ERR_INVALID_ARG, "null argument");
-  for (uint32_t i = 0; i < m; ++i) {
-    mistic_status s = mistic_selfjoin(h, inst[i].pts, inst[i].n, inst[i].d, inst[i].dtype, inst[i].k,
-                                      inst[i].eps, opts, &results[i]);
-    if (s != MISTIC_OK) return s;
+  unsigned want = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+  if (const char* e = getenv("MISTIC_BATCH_STREAMS")) want = (unsigned)std::max(1l, strtol(e, nullptr, 10));
+  const unsigned W = std::min<unsigned>(want, m);
+  if (W <= 1 || (opts && opts->pair_buffer)) {
+    for (uint32_t i = 0; i < m; ++i) {
+      mistic_status s = mistic_selfjoin(h, inst[i].pts, inst[i].n, inst[i].d, inst[i].dtype, inst[i].k,
+                                        inst[i].eps, opts, &results[i]);
+      if (s != MISTIC_OK) return s;
+    }
+    return MISTIC_OK;
   }
+  memset(results, 0, sizeof(mistic_result) * m);
+  try {
+    MCK(cudaSetDevice(h->device));
+    while (h->workers.size() < W) {
+      mistic_handle w = nullptr;
+      const mistic_status s = mistic_create(&w, h->device, nullptr);
+      if (s != MISTIC_OK) throw Error(s, "batch worker handle");
+      h->workers.push_back(w);
+    }
+    if (!h->batch_ev) MCK(cudaEventCreateWithFlags(&h->batch_ev, cudaEventDisableTiming));
+    MCK(cudaEventRecord(h->batch_ev, h->stream));  // inputs produced on the caller's stream
+    for (unsigned t = 0; t < W; ++t) MCK(cudaStreamWaitEvent(h->workers[t]->stream, h->batch_ev, 0));
+  } catch (const Error& e) {
+    return fail(h, e.status, e.what());
+  }
+  std::atomic<uint32_t> next{0};
+  std::atomic<bool> stop{false};
+  std::mutex mu;
+  uint32_t err_i = UINT32_MAX;
+  mistic_status err_s = MISTIC_OK;
+  std::string err_msg;
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < W; ++t) {
+    th.emplace_back([&, t]() {
+      mistic_handle w = h->workers[t];
+      cudaSetDevice(h->device);
+      for (;;) {
+        const uint32_t i = next.fetch_add(1);
+        if (i >= m || stop.load()) break;
+        const mistic_status s = mistic_selfjoin(w, inst[i].pts, inst[i].n, inst[i].d, inst[i].dtype, inst[i].k,
+                                                inst[i].eps, opts, &results[i]);
+        if (s != MISTIC_OK) {
+          std::lock_guard<std::mutex> g(mu);
+          if (i < err_i) {
+            err_i = i;
+            err_s = s;
+            err_msg = w->last_error;
+          }
+          stop.store(true);
+        }
+      }
+    });
+  }
+  for (auto& x : th) x.join();
+  if (err_s != MISTIC_OK) return fail(h, err_s, err_msg.c_str());
   return MISTIC_OK;
 }
 

@@ -17,7 +17,7 @@ import numpy as np
 
 from . import _lib as L
 
-__all__ = ["MisticError", "JoinResult", "Handle", "selfjoin", "read_points"]
+__all__ = ["MisticError", "JoinResult", "Handle", "selfjoin", "read_points", "convert_text"]
 
 MODES = {"auto": L.MODE_AUTO, "fp64": L.MODE_FP64, "fp32": L.MODE_FP32, "bf16": L.MODE_BF16}
 RP_MODES = {"pca": L.RP_PCA, "box": L.RP_BOX, "user": L.RP_USER}
@@ -173,6 +173,28 @@ class Handle:
         r = self.selfjoin_raw(a.ctypes.data if n else 0, n, d, dt, k, eps, o)
         return self.to_result(r)
 
+    def batch_selfjoin(self, instances, **kw) -> list[JoinResult]:
+        """mistic_batch_selfjoin over [(pts, k, eps), ...] host arrays; one
+        result per instance, in order."""
+        arrs, inst = [], (L.Instance * max(1, len(instances)))()
+        for i, (pts, k, eps) in enumerate(instances):
+            a = np.ascontiguousarray(pts)
+            if a.dtype not in (np.float64, np.float32):
+                a = a.astype(np.float64)
+            arrs.append(a)
+            inst[i].pts = a.ctypes.data if a.shape[0] else None
+            inst[i].n, inst[i].d = a.shape
+            inst[i].dtype = L.F64 if a.dtype == np.float64 else L.F32
+            inst[i].k, inst[i].eps = k, float(eps)
+        res = (L.Result * max(1, len(instances)))()
+        o = self.opts(**kw)
+        st = self.lib.mistic_batch_selfjoin(self.h, inst, len(instances), ctypes.byref(o), res)
+        if st != L.OK:
+            for i in range(len(instances)):
+                self.lib.mistic_result_free(ctypes.byref(res[i]))
+        _check(self.lib, self.h, st)
+        return [self.to_result(res[i]) for i in range(len(instances))]
+
     def free_result(self, jr: JoinResult) -> None:
         raw = jr.extra.pop("_raw", None)
         if raw is not None:
@@ -203,3 +225,14 @@ def read_points(path: str, d: int, dtype: str = "f64") -> np.ndarray:
         arr = np.zeros((0, d), dtype=npdt)
     lib.mistic_free_host(p)
     return arr
+
+
+def convert_text(text_path: str, bin_path: str) -> int:
+    """Text -> raw FP64 point file (the reference's toBin behaviour, see
+    mistic_convert_text); returns the number of values written."""
+    lib = L.load()
+    n = ctypes.c_uint64()
+    st = lib.mistic_convert_text(text_path.encode(), bin_path.encode(), ctypes.byref(n))
+    if st != L.OK:
+        raise MisticError(st, lib.mistic_strerror(st).decode())
+    return int(n.value)

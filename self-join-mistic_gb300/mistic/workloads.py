@@ -135,10 +135,49 @@ def gen_clusters(n: int, d: int, n_clusters: int, seed: int,
         pos += m
     perm = rng.permutation(n)
     out = out[perm]
-    if normalise:
-        nrm = np.linalg.norm(out.astype(np.float64), axis=1, keepdims=True)
-        out = (out / nrm).astype(dtype)
+    if normalise:  # row L2 norms in FP64 (same bits as np.linalg.norm), in chunks
+        for r0 in range(0, n, 1 << 16):
+            blk = out[r0:r0 + (1 << 16)].astype(np.float64)
+            nrm = np.sqrt(np.add.reduce(blk * blk, axis=1, keepdims=True))
+            out[r0:r0 + (1 << 16)] = (blk / nrm).astype(dtype)
     return out
+
+
+def gen_clusters_device(n: int, d: int, n_clusters: int, seed: int, zipf: float = 1.1,
+                        eig_lo: float = 1e-3, eig_hi: float = 1.0, device: str = "cuda"):
+    """The generator of gen_clusters (Zipf cluster sizes, low-rank random
+    rotation x log-uniform eigenvalues plus an isotropic floor, rows
+    L2-normalised), drawn with a seeded torch generator on the GPU so that a
+    5M x 384 set takes seconds instead of many minutes.  Returns an FP32
+    host array.  The values differ from gen_clusters (another random
+    stream); ε is calibrated on the result."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    w = 1.0 / torch.arange(1, n_clusters + 1, dtype=torch.float64) ** zipf
+    sizes = np.random.default_rng(seed).multinomial(n, (w / w.sum()).numpy())
+    out = torch.empty((n, d), dtype=torch.float32, device=device)
+    centres = torch.randn((n_clusters, d), generator=g, device=device, dtype=torch.float32)
+    r = min(d, 32)
+    pos = 0
+    for c in range(n_clusters):
+        m = int(sizes[c])
+        if m == 0:
+            continue
+        basis, _ = torch.linalg.qr(torch.randn((d, r), generator=g, device=device, dtype=torch.float32))
+        u = torch.rand((r,), generator=g, device=device, dtype=torch.float32)
+        eig = torch.exp(math.log(eig_lo) + u * (math.log(eig_hi) - math.log(eig_lo)))
+        z = torch.randn((m, r), generator=g, device=device, dtype=torch.float32) * eig.sqrt()
+        blk = centres[c] * 0.5 + z @ basis.T
+        blk += torch.randn((m, d), generator=g, device=device, dtype=torch.float32) * math.sqrt(eig_lo)
+        out[pos:pos + m] = blk
+        pos += m
+    out = out[torch.randperm(n, generator=g, device=device)]
+    out /= out.double().norm(dim=1, keepdim=True).float()
+    host = out.cpu().numpy()
+    del out
+    torch.cuda.empty_cache()
+    return host
 
 
 # ---------------------------------------------------------------- ε calibration
@@ -247,9 +286,87 @@ def msd90(n: int = 515_345) -> Workload:
 
 
 def tiny384(n: int = 5_000_000) -> Workload:
-    pts = gen_clusters(n, 384, 1000, seed=5, zipf=1.1, normalise=True)
-    key = f"tiny384:{n}"
+    """TINY-shaped: FP32, d = 384, 1,000 Zipf(1.1) clusters, L2-normalised
+    rows, k = 8, 16 mean neighbours.  Large sets are drawn on the GPU."""
+    try:
+        import torch
+        on_gpu = n >= 200_000 and torch.cuda.is_available()
+    except ImportError:
+        on_gpu = False
+    if on_gpu:
+        pts = gen_clusters_device(n, 384, 1000, seed=5)
+    else:
+        pts = gen_clusters(n, 384, 1000, seed=5, zipf=1.1, normalise=True)
+    key = f"tiny384:{n}:{'gpu' if on_gpu else 'np'}"
     return Workload(key, pts, 8, _eps_for(key, pts, 16.0), 16.0)
+
+
+def _calibrate_eps_device(x, target_mean: float, sample: int, seed: int, iters: int = 60) -> float:
+    """calibrate_eps on a device tensor: the same estimator and bisection,
+    with the sample's FP64 squared distances computed and sorted on the GPU."""
+    import torch
+    n = x.shape[0]
+    m = min(sample, n)
+    g = torch.Generator(device=x.device)
+    g.manual_seed(seed)
+    idx = torch.sort(torch.randperm(n, generator=g, device=x.device)[:m]).values
+    s = x[idx].double()
+    nrm = (s * s).sum(dim=1)
+    d2 = (nrm[:, None] + nrm[None, :] - 2.0 * (s @ s.T))
+    iu = torch.triu_indices(m, m, offset=1, device=x.device)
+    d2 = torch.sort(d2[iu[0], iu[1]].clamp_min_(0.0)).values
+    scale = (n - 1) / max(m - 1, 1)
+    top = float(d2[-1].item()) if d2.numel() else 0.0
+    lo, hi = 0.0, math.sqrt(top) * 1.0001 + 1e-300
+    for _ in range(iters):
+        mid = 0.5 * (lo + hi)
+        cnt = int(torch.searchsorted(d2, torch.tensor([mid * mid], dtype=torch.float64, device=x.device),
+                                     right=True).item())
+        if 2.0 * cnt / m * scale >= target_mean:
+            hi = mid
+        else:
+            lo = mid
+    return hi
+
+
+def batch_instances_device(count: int = 2000, seed: int = 7, n_lo: int = 1_000, n_hi: int = 200_000,
+                           device: str = "cuda") -> list[Workload]:
+    """The instance mix of batch_instances (same n, d, cluster count and
+    target per index), with the points drawn and ε calibrated on the GPU so
+    that 2,000 instances take seconds.  FP32 host arrays."""
+    import torch
+    master = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(round(math.exp(master.uniform(math.log(n_lo), math.log(n_hi)))))
+        d = int(master.choice([2, 8, 18, 32, 57, 90]))
+        nc = int(master.integers(1, 51))
+        tgt = float(master.choice([4.0, 16.0, 64.0]))
+        rng = np.random.default_rng(seed * 100_003 + i)
+        w = rng.random(nc) + 0.1
+        sizes = rng.multinomial(n, w / w.sum())
+        g = torch.Generator(device=device)
+        g.manual_seed(seed * 100_003 + i)
+        x = torch.empty((n, d), dtype=torch.float32, device=device)
+        centres = torch.randn((nc, d), generator=g, device=device)
+        r = min(d, 32)
+        pos = 0
+        for c in range(nc):
+            m = int(sizes[c])
+            if m == 0:
+                continue
+            basis, _ = torch.linalg.qr(torch.randn((d, r), generator=g, device=device))
+            u = torch.rand((r,), generator=g, device=device)
+            eig = torch.exp(math.log(1e-2) + u * (0.0 - math.log(1e-2)))
+            z = torch.randn((m, r), generator=g, device=device) * eig.sqrt()
+            blk = centres[c] * 0.5 + z @ basis.T
+            blk += torch.randn((m, d), generator=g, device=device) * 0.1
+            x[pos:pos + m] = blk
+            pos += m
+        x = x[torch.randperm(n, generator=g, device=device)]
+        eps = _calibrate_eps_device(x, tgt, sample=min(n, 4000), seed=i)
+        out.append(Workload(f"batch{i}", x.cpu().numpy(), min(6, d), eps, tgt, {"index": i}))
+    return out
 
 
 def batch_instances(count: int = 2000, seed: int = 7, n_lo: int = 1_000,

@@ -58,6 +58,13 @@ def golden():
 
 
 @pytest.fixture(scope="session")
+def golden_full():
+    import json
+    with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+        return json.load(f)["full_size"]
+
+
+@pytest.fixture(scope="session")
 def handle():
     import mistic
     h = mistic.Handle(0)

@@ -91,35 +91,61 @@ CASES = [
 ]
 
 
+# Full-size cases (the c1 workload: n = 100,000, d = 18, U[0,1) from seed 0,
+# ε calibrated to 32 mean neighbours).  `--full` (re)computes only these and
+# keeps the small cases; the reference's brute force takes about 30 s here.
+FULL_CASES = [
+    dict(name="c1_uniform18_n100000", gen="uniform", n=100000, d=18, seed=0, k=6, eps_hex="0x1.c37b06bdae65ep-1"),
+]
+
+
+def pin(c: dict) -> dict:
+    x = gen_case(c)
+    if c.get("f32"):
+        x = x.astype(np.float32)
+    if "eps_hex" in c:
+        eps = float.fromhex(c["eps_hex"])
+    else:
+        eps = c["eps"] if "eps" in c else W.calibrate_eps(x.astype(np.float64), c["target"])
+    x64 = x.astype(np.float64)
+    with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
+        path = f.name
+    W.write_bin(path, x64)
+    r = subprocess.run([REF, path, str(c["d"]), repr(float(eps))], capture_output=True, text=True, check=True)
+    os.unlink(path)
+    ref = json.loads(r.stdout.strip().splitlines()[-1])
+    pairs, amb = O.brute_pairs(x, eps, want_ambig=True)
+    rec = dict(c)
+    rec.update(eps_hex=float(eps).hex(), input_sha256=input_sha(x), ref_ordered_incl_self=ref["ordered_incl_self"],
+               oracle_pairs_ij=int(len(pairs)), oracle_pairs_sha256=pairs_sha(pairs), ulp_ambiguous=int(amb))
+    assert 2 * len(pairs) + c["n"] == ref["ordered_incl_self"], (c["name"], len(pairs), ref)
+    print(c["name"], len(pairs), ref["ordered_incl_self"], "amb", amb, flush=True)
+    return rec
+
+
 def main() -> None:
     if not os.path.exists(REF):
         sys.exit("oracle/_ref/ref_brute missing: run oracle/build_ref.sh first")
+    path = os.path.join(HERE, "golden.json")
+    if "--full" in sys.argv:
+        with open(path) as f:
+            g = json.load(f)
+        g["full_size"] = [pin(c) for c in FULL_CASES]
+        with open(path, "w") as f:
+            json.dump(g, f, indent=1)
+        return
     out = []
     for c in CASES:
-        x = gen_case(c)
-        if c.get("f32"):
-            x = x.astype(np.float32)
-        eps = c["eps"] if "eps" in c else W.calibrate_eps(x.astype(np.float64), c["target"])
-        x64 = x.astype(np.float64)
-        with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
-            path = f.name
-        W.write_bin(path, x64)
-        r = subprocess.run([REF, path, str(c["d"]), repr(float(eps))], capture_output=True, text=True,
-                           check=True)
-        os.unlink(path)
-        ref = json.loads(r.stdout.strip().splitlines()[-1])
-        pairs, amb = O.brute_pairs(x, eps, want_ambig=True)
-        rec = dict(c)
-        rec.update(eps_hex=float(eps).hex(), input_sha256=input_sha(x),
-                   ref_ordered_incl_self=ref["ordered_incl_self"], oracle_pairs_ij=int(len(pairs)),
-                   oracle_pairs_sha256=pairs_sha(pairs), ulp_ambiguous=int(amb))
-        assert 2 * len(pairs) + c["n"] == ref["ordered_incl_self"], (c["name"], len(pairs), ref)
-        print(c["name"], len(pairs), ref["ordered_incl_self"], "amb", amb, flush=True)
-        out.append(rec)
-    with open(os.path.join(HERE, "golden.json"), "w") as f:
-        json.dump({"generator": "tests/golden/make_golden.py",
-                   "reference_binary": "oracle/_ref/ref_brute (src/utils.cu:285-317, unmodified)",
-                   "cases": out}, f, indent=1)
+        out.append(pin(c))
+    g = {"generator": "tests/golden/make_golden.py",
+         "reference_binary": "oracle/_ref/ref_brute (src/utils.cu:285-317, unmodified)", "cases": out}
+    if os.path.exists(path):
+        with open(path) as f:
+            old = json.load(f)
+        if "full_size" in old:
+            g["full_size"] = old["full_size"]
+    with open(path, "w") as f:
+        json.dump(g, f, indent=1)
 
 
 if __name__ == "__main__":

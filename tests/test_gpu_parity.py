@@ -38,6 +38,20 @@ def test_golden_case(handle, golden, idx, mode):
     assert r.ulp_ambiguous == c["ulp_ambiguous"]
 
 
+@pytest.mark.parametrize("mode", MODES)
+def test_c1_full_size(handle, golden_full, mode):
+    """The c1 workload at full size (n = 100,000, d = 18): the reference's
+    own brute-force count and the oracle's pair-list hash, in every mode."""
+    c = golden_full[0]
+    x = case_input(c)
+    assert input_sha(x) == c["input_sha256"]
+    r = run(handle, x, c["k"], float.fromhex(c["eps_hex"]), mode=mode)
+    assert r.pairs_ordered_incl_self == c["ref_ordered_incl_self"] == 3293520
+    assert r.pairs_ij == c["oracle_pairs_ij"]
+    assert pairs_sha(r.pairs) == c["oracle_pairs_sha256"]
+    assert r.ulp_ambiguous == c["ulp_ambiguous"]
+
+
 @pytest.mark.parametrize("rp", ["pca", "box"])
 @pytest.mark.parametrize("k", [1, 3, 6, 8, 16])
 def test_reference_point_choices_agree(handle, rp, k):

@@ -35,6 +35,18 @@ def test_oracle_matches_reference_counts(golden, idx):
         assert (pairs[:, 0] < pairs[:, 1]).all()
 
 
+def test_full_size_pin_is_consistent(golden_full):
+    """The c1 pin (reference brute force over 100,000 x 18 points): its input
+    regenerates bit-for-bit here, and the reference's ordered count equals
+    2 x the oracle's i<j pairs + n."""
+    c = golden_full[0]
+    x = case_input(c)
+    assert x.shape == (100000, 18)
+    if input_sha(x) != c["input_sha256"]:
+        pytest.skip("generator output differs from the fixture on this numpy")
+    assert c["ref_ordered_incl_self"] == 2 * c["oracle_pairs_ij"] + c["n"] == 3293520
+
+
 def test_ordered_count_is_reference_number(golden):
     c = golden[0]
     x = case_input(c)
