@@ -450,7 +450,7 @@ def run_batch(args) -> None:
         t_s, cost_s = 0.0, 0.0
         for i in list(range(0, m, max(1, m // 8)))[:8]:
             x = xs[i]
-            rows = min(x.shape[0], max(64, int(2e8 / max(1, x.shape[0] * x.shape[1]))))
+            rows = min(x.shape[0], max(256, int(args.cpu_seconds * 2e9 / 8 / max(1, x.shape[0] * x.shape[1]))))
             t0 = time.perf_counter()
             O.count_rows(x, wls[i].eps, 0, rows, threads)
             t_s += time.perf_counter() - t0

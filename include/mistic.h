@@ -191,6 +191,17 @@ mistic_status mistic_read_points(const char* path, uint32_t d, mistic_dtype dtyp
                                  void** out_pts, uint64_t* out_n);
 void mistic_free_host(void* p);
 
+/* GPU FP64 brute force over rows [row0, row1) against all n points: counts
+ * [i - row0] = number of j != i whose reference predicate s(i, j) <= fl(ε*ε)
+ * holds (src/utils.cu:296-309; the reference's GPU brute force is dumbBrute,
+ * src/kernel.cu:1243-1261).  A subsample oracle at sizes where the CPU brute
+ * force cannot run: for a sample of rows these counts must equal the
+ * neighbour-table degrees minus the self edge.  `counts` is a host array of
+ * row1 - row0 entries; `pts` is host memory unless input_on_device. */
+mistic_status mistic_bruteforce_rows(mistic_handle h, const void* pts, uint64_t n, uint32_t d,
+                                    mistic_dtype dtype, double eps, uint64_t row0, uint64_t row1,
+                                    int input_on_device, uint32_t* counts);
+
 /* Text -> binary converter with the behaviour of the reference's toBin tool
  * (toCSV.cpp:52-85): reads decimal numbers separated by commas and/or white
  * space from `text_path`, stopping at the first token that is not a number,

@@ -493,12 +493,10 @@ void sample_cov(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, ui
 void rp_dist(mistic_handle_s* h, const void* x, mistic_dtype dt, size_t n, uint32_t d,
              const double* rps, int k, double* D, double* part, uint32_t nparts, double* mm) {
   const size_t smem = (size_t)k * d * sizeof(double) + (d <= RPD_DMAX ? (size_t)RPD_THREADS * d * sizeof(double) : 0);
-  if (smem > 48 * 1024) {
-    if (dt == MISTIC_F64)
-      allow_max_dyn_smem(k_rp_dist<double>);
-    else
-      allow_max_dyn_smem(k_rp_dist<float>);
-  }
+  if (dt == MISTIC_F64)  // the limit includes static shared memory: raise it whatever the size
+    allow_max_dyn_smem(k_rp_dist<double>);
+  else
+    allow_max_dyn_smem(k_rp_dist<float>);
   if (dt == MISTIC_F64)
     k_rp_dist<double><<<nparts, RPD_THREADS, smem, h->stream>>>((const double*)x, n, d, rps, k, D, part);
   else

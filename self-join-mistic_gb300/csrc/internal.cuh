@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <stdexcept>
@@ -79,7 +80,7 @@ struct JoinCounters {
   unsigned long long tiles;      // tensor-core tiles evaluated
   unsigned long long cells;      // sum over those tiles of home rows x candidate columns
   unsigned long long band_n;     // candidate pairs appended to the band list (decided afterwards in FP64)
-  unsigned long long prof[16];   // role cycle breakdown when TcParams.prof is set
+  unsigned long long prof[24];   // role cycle breakdown when TcParams.prof is set
 };
 
 // Key packing: field f = floor((D[i*kstride + col[f]] - dmin[f]) / w[f]),
@@ -233,6 +234,11 @@ int tc_kp(uint32_t d);
 uint32_t tc_rows(uint32_t d);
 void run_tc(mistic_handle_s*, const JoinParams&, const TcParams&);
 }  // namespace join
+
+// ---- brute.cu: FP64 brute-force neighbour counts of rows [row0, row1)
+// against all n rows (device input, device counts).
+void bruteforce_rows(mistic_handle_s* h, const void* x, mistic_dtype dt, uint64_t n, uint32_t d, double eps2,
+                     uint64_t row0, uint64_t row1, uint32_t* counts);
 
 // ---- rp.cpp: reference-point selection on the host.
 // stats: per-dim mean (d), min (d), max (d); cov: d x d sample covariance.

@@ -401,6 +401,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
     uint32_t tile = 0, issued = 0, unit_k = 0, pf = 0;
     unsigned long long n_tiles = 0, n_cells = 0;
     long long pw_sfree = 0, pc_unit = 0, pc_win = 0, pc_conv = 0, pc_ldw = 0;
+    long long pc_adv = 0, pc_bar = 0, pc_p1 = 0, pc_p2 = 0, pc_fin = 0;
     uint32_t wgen = 0;  // window refills so far (tags S.w_home)
     // tiles in flight: RAW landing slots, or (rows landing in the B stages
     // themselves) NS - 1, so that issuing tile t + LA - 1 waits only on tiles
@@ -515,6 +516,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
           seg_next += nb;
           if (T.prof) pc_win += clock64() - cw0;
         }
+        const long long ca0 = T.prof ? clock64() : 0;
         const uint32_t ncols = min((uint32_t)TN, w_total - w_pos);
         const bool last = (w_pos + TN >= w_total) && (seg_next >= U.s1);
         uint32_t q = 0xffffffffu;
@@ -574,6 +576,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         }
         w_pos += TN;
         ++issued;
+        if (T.prof) pc_adv += clock64() - ca0;
         return 1;
       };
 
@@ -607,12 +610,14 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
           sh = Raw + rs * 2 * OPB;
           sl = sh + OPB;
           const uint32_t fl = pf++ & 1;
+          const long long cb0 = T.prof ? clock64() : 0;
           if (tid == 0) {
             const long long c0 = T.prof ? clock64() : 0;
             S.pflag[fl] = wait_or_abort(&S.sfree[st], ((tile / NS) & 1) ^ 1, abort_flag, T.wait_limit) ? 1u : 0u;
             if (T.prof) pw_sfree += clock64() - c0;
           }
           prod_sync();
+          if (T.prof) pc_bar += clock64() - cb0;
           if (!S.pflag[fl]) {
             aborted = true;
             break;
@@ -620,6 +625,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
           if (half == 0) S.qid[st][prow] = id;
         }
         const bool ok = prow < ncols;
+        const long long cp0 = T.prof ? clock64() : 0;
         const float part = conv_pass1<KP>(sh, sl, bh, bl, prow, half, ok, S.cadd_b, -2.f, P.d);
         const float nq2 = (part + __shfl_xor_sync(FULL_MASK, part, 16)) * 0.25f;
         float tcol = 0.f, dl = 0.f;
@@ -627,7 +633,13 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
           tcol = 1e30f;   // every row of this column becomes a candidate ...
           dl = INFINITY;  // ... and none is accepted without the FP64 check
         }
+        const long long cp1 = T.prof ? clock64() : 0;
         conv_pass2<KP>(sh, sl, bh, bl, prow, half, ok, S.cadd_b, -2.f, P.d, 1.f, nq2 - tcol);
+        const long long cp2 = T.prof ? clock64() : 0;
+        if (T.prof) {
+          pc_p1 += cp1 - cp0;
+          pc_p2 += cp2 - cp1;
+        }
         if (half == 0) S.dlt[st][prow] = dl;
 #pragma unroll
         for (int i = 0; i < (G + 1) / 2; ++i)
@@ -640,7 +652,11 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive(&S.full[st]);
-        if (T.prof) pc_conv += clock64() - cc0;
+        if (T.prof) {
+          const long long ce = clock64();
+          pc_fin += ce - cp2;
+          pc_conv += ce - cc0;
+        }
         first = false;
         ++tile;
       }
@@ -662,6 +678,11 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
       atomicAdd(&T.ctr->prof[8], (unsigned long long)pc_win);
       atomicAdd(&T.ctr->prof[9], (unsigned long long)pc_conv);
       atomicAdd(&T.ctr->prof[14], (unsigned long long)pc_ldw);
+      atomicAdd(&T.ctr->prof[16], (unsigned long long)pc_adv);
+      atomicAdd(&T.ctr->prof[17], (unsigned long long)pc_bar);
+      atomicAdd(&T.ctr->prof[18], (unsigned long long)pc_p1);
+      atomicAdd(&T.ctr->prof[19], (unsigned long long)pc_p2);
+      atomicAdd(&T.ctr->prof[20], (unsigned long long)pc_fin);
     }
   } else if (warp == MMA_WARP) {
     // ============================ MMA issuer

@@ -654,6 +654,12 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
               tot_e ? 100.0 * tcc.prof[10] / tot_e : 0.0,
               tot_e ? 100.0 * tcc.prof[11] / tot_e : 0.0, tot_e ? 100.0 * tcc.prof[13] / tot_e : 0.0,
               (unsigned long long)tcc.tiles, (unsigned long long)tcc.prof[12]);
+      fprintf(stderr,
+              "[mistic] join_tc producer steps (thread 0): advance %.1f%% | stage wait + barrier %.1f%% | pass 1 + "
+              "norm + threshold %.1f%% | pass 2 %.1f%% | metadata + fence + arrive %.1f%%\n",
+              tot_p ? 100.0 * tcc.prof[16] / tot_p : 0.0, tot_p ? 100.0 * tcc.prof[17] / tot_p : 0.0,
+              tot_p ? 100.0 * tcc.prof[18] / tot_p : 0.0, tot_p ? 100.0 * tcc.prof[19] / tot_p : 0.0,
+              tot_p ? 100.0 * tcc.prof[20] / tot_p : 0.0);
     }
   }
 
@@ -891,6 +897,29 @@ mistic_status mistic_destroy(mistic_handle h) {
   if (h->batch_ev) cudaEventDestroy(h->batch_ev);
   delete h;
   return MISTIC_OK;
+}
+
+mistic_status mistic_bruteforce_rows(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mistic_dtype dtype,
+                                    double eps, uint64_t row0, uint64_t row1, int input_on_device,
+                                    uint32_t* counts) {
+  MISTIC_GUARD(h, {
+    mistic::check_handle(h);
+    if (d == 0 || (n > 0 && !pts) || !counts || row0 > row1 || row1 > n)
+      throw mistic::Error(MISTIC_ERR_INVALID_ARG, "bad brute-force arguments");
+    if (dtype != MISTIC_F64 && dtype != MISTIC_F32) throw mistic::Error(MISTIC_ERR_INVALID_ARG, "bad dtype");
+    if (!(eps >= 0.0) || !std::isfinite(eps)) throw mistic::Error(MISTIC_ERR_INVALID_ARG, "eps must be finite and >= 0");
+    if (row1 == row0) return MISTIC_OK;
+    const size_t esz = dtype == MISTIC_F64 ? 8 : 4;
+    const void* x = pts;
+    if (!input_on_device) {
+      void* dx = h->arena.get("bf_raw", n * d * esz);
+      mistic::h2d(h, dx, pts, n * d * esz);
+      x = dx;
+    }
+    uint32_t* dc = (uint32_t*)h->arena.get("bf_counts", (row1 - row0) * sizeof(uint32_t));
+    mistic::bruteforce_rows(h, x, dtype, n, d, eps * eps, row0, row1, dc);
+    mistic::d2h(h, counts, dc, (row1 - row0) * sizeof(uint32_t));
+  });
 }
 
 mistic_status mistic_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mistic_dtype dtype,

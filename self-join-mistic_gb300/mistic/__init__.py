@@ -195,6 +195,26 @@ class Handle:
         _check(self.lib, self.h, st)
         return [self.to_result(res[i]) for i in range(len(instances))]
 
+    def bruteforce_rows(self, pts, eps: float, row0: int, row1: int, on_device_ptr: int | None = None,
+                        n: int | None = None, d: int | None = None, dtype: int | None = None) -> np.ndarray:
+        """FP64 brute-force neighbour counts (self excluded) of rows
+        [row0, row1) against all rows, on the GPU (mistic_bruteforce_rows).
+        `pts` is a host array, or pass on_device_ptr with n, d, dtype."""
+        out = np.zeros(max(0, row1 - row0), dtype=np.uint32)
+        if on_device_ptr is None:
+            a = np.ascontiguousarray(pts)
+            if a.dtype not in (np.float64, np.float32):
+                a = a.astype(np.float64)
+            n, d = a.shape
+            dtype = L.F64 if a.dtype == np.float64 else L.F32
+            ptr, dev = a.ctypes.data, 0
+        else:
+            ptr, dev = on_device_ptr, 1
+        st = self.lib.mistic_bruteforce_rows(self.h, ctypes.c_void_p(ptr), n, d, dtype, float(eps), row0, row1, dev,
+                                             out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+        _check(self.lib, self.h, st)
+        return out
+
     def free_result(self, jr: JoinResult) -> None:
         raw = jr.extra.pop("_raw", None)
         if raw is not None:

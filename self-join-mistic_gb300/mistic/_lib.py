@@ -29,7 +29,7 @@ EXPORTS = (
     "mistic_abi_version", "mistic_opts_init", "mistic_create", "mistic_destroy",
     "mistic_selfjoin", "mistic_batch_selfjoin", "mistic_read_points",
     "mistic_free_host", "mistic_result_free", "mistic_strerror",
-    "mistic_last_error", "mistic_selfjoin_noalloc", "mistic_convert_text",
+    "mistic_last_error", "mistic_selfjoin_noalloc", "mistic_convert_text", "mistic_bruteforce_rows",
 )
 
 #: scratch limits of mistic_selfjoin_noalloc (include/mistic.h)
@@ -128,6 +128,9 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
     L.mistic_read_points.argtypes = [ctypes.c_char_p, u32, ctypes.c_int,
                                      ctypes.POINTER(vp), ctypes.POINTER(u64)]
     L.mistic_read_points.restype = ctypes.c_int
+    L.mistic_bruteforce_rows.argtypes = [vp, vp, u64, u32, ctypes.c_int, dbl, u64, u64, ctypes.c_int,
+                                         ctypes.POINTER(u32)]
+    L.mistic_bruteforce_rows.restype = ctypes.c_int
     L.mistic_convert_text.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(u64)]
     L.mistic_convert_text.restype = ctypes.c_int
     L.mistic_free_host.argtypes = [vp]
