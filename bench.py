@@ -82,6 +82,11 @@ WORKLOADS = {
 
 FALLBACK_PEAKS = {"hbm_gbs": 6785.9, "bf16_tflops": 1922.1, "bf16_tflops_sustained": 1711.2}
 
+#: DRAM bytes (read + write) per evaluated cell of k_join_tc on the SUSY-shaped
+#: data, from the ncu capture of the 2.5M-point case (profiles/join_tc_susy18.md:
+#: 283.8 MB over 2.1993e10 cells); scaled by the cells of the measured launch.
+TC_DRAM_BYTES_PER_CELL_SUSY18 = 283.8e6 / 2.1993e10
+
 
 def load_peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -318,6 +323,10 @@ def run_mistic(args, wl) -> None:
                 "traffic": None, "work": "2*d flops per evaluated cell (one d-long contraction)",
                 "peak_source": peaks["_source"] + " bf16 burst (of measured)", "kernel_ms": tc_ms,
                 "cells": r.tc_cells, "fp32_simt_peak_tflops": fp32_peak}
+        if args.workload == "susy18":
+            roof["traffic"] = TC_DRAM_BYTES_PER_CELL_SUSY18 * r.tc_cells
+            roof["traffic_source"] = ("ncu dram__bytes_read+write per cell of the 2.5M-point capture "
+                                      "(profiles/join_tc_susy18.md) x this launch's cells")
     else:
         # dominant kernel: the FP32 filter join; 3*d flops per candidate pair
         # (d subtractions, d multiply-adds) on the CUDA-core FP32 pipe
