@@ -27,14 +27,13 @@
 // with sum_k |A_k||B_k| <= (|a'| + |q'|)^2.  Rows whose bound exceeds
 // 0.1 eps2 are re-decided entirely in FP64 (T_lo = -1, T_hi = inf).
 //
-// Data movement: operands are converted from the sorted FP32 rows by the
-// CTA's threads straight into the no-swizzle K-major core-matrix layout
-// (8 rows x 16 bytes per core matrix; LBO = 128 B between K-adjacent core
-// matrices, SBO = 16*KP B between 8-row groups), then one elected thread
-// issues the MMAs and commits to an mbarrier; all 8 warps read the 128 x 128
-// FP32 tile back with tcgen05.ld (warp w: TMEM lanes 32*(w%4).., columns
-// 64*(w/4)..).  Every mbarrier wait is bounded; on expiry the CTA records
-// an error, stops, and releases its tensor memory.
+// Data movement: operands are converted from the sorted FP32 rows into the
+// no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix;
+// LBO = 128 B between K-adjacent core matrices, SBO = 16*KP B between 8-row
+// groups), one elected thread issues the MMAs and commits to an mbarrier,
+// and the epilogue warps read each 128 x 128 FP32 accumulator back with
+// tcgen05.ld.  Every mbarrier wait is bounded; on expiry the CTA records an
+// error, stops, drains its MMAs and releases its tensor memory.
 #include <cuda_bf16.h>
 #include <math.h>
 
@@ -101,21 +100,25 @@ __device__ __forceinline__ uint32_t warp_scan_incl(uint32_t x) {
 }
 
 // ---------------------------------------------------------------- pipeline
-// One CTA = 9 warps:
-//   warps 0-3  producers: fetch units, convert the unit's home rows (A, once
-//              per unit) and each tile's 128 candidate rows (B) into a ring of
-//              NS shared-memory stages, with the per-column threshold folded
-//              into B (column d+1 holds |q'|^2 - T(n));
-//   warp 8     MMA issuer (one lane): 3 * KP/16 tcgen05.mma per tile into one
-//              of two TMEM accumulators, tcgen05.commit to signal completion;
-//   warps 4-7  epilogue: tcgen05.ld of TMEM lanes 32*(w-4).., sign-bit test
-//              (D' < 0 marks a candidate), exact decision, pair emission.
-// Barriers (all waits bounded):
-//   full[s]   producers -> MMA        (128 arrivals)
-//   sfree[s]  epilogue  -> producers  (4 arrivals; stage s and its metadata reusable)
+// One persistent CTA per SM: 8 producer warps, NEPI epilogue warps, 1 MMA warp.
+//   producers  fetch units; stage the unit's home rows (A: G chunks of 128,
+//              once per unit) and each tile's 128 candidate rows (B) in an
+//              NS-stage ring, two threads per row: raw FP32 rows arrive by
+//              cp.async (in a RAW-slot landing ring, or in the B stage
+//              itself) and are converted in place into bf16 hi/lo with the
+//              per-column threshold folded into B (column d+1 holds
+//              |q'|^2 - T(n)); up to LA tiles are in flight;
+//   MMA warp   one lane issues 3 * KP/16 tcgen05.mma per (tile, home chunk)
+//              into the next of NACC = 4 TMEM accumulators and commits;
+//   epilogue   tcgen05.ld of TMEM lane quarter w % 4, sign-bit test (D' < 0
+//              marks a candidate), home-bin rule by column range, sure
+//              accepts to the pair list, the error band to the band list.
+// Barriers (all waits bounded by a %globaltimer deadline):
+//   full[s]   producers -> MMA        (NPROD arrivals)
+//   sfree[s]  epilogue  -> producers  (NEPI arrivals after the tile's last home chunk)
 //   dfull[b]  MMA       -> epilogue   (tcgen05.commit, or a plain arrive on the terminate tile)
-//   dfree[b]  epilogue  -> MMA        (4 arrivals; accumulator b reusable)
-//   afull     producers -> MMA        (128 arrivals per unit: A written)
+//   dfree[b]  epilogue  -> MMA        (NEPI arrivals; accumulator b reusable)
+//   afull     producers -> MMA        (NPROD arrivals per unit: A written)
 //   afree     MMA       -> producers  (tcgen05.commit after a unit's last tile)
 constexpr int NPW = 8;     // producer warps: two threads per operand row
 constexpr int NPROD = NPW * 32;
