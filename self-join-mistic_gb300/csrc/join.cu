@@ -183,34 +183,32 @@ __device__ __forceinline__ CandTile next_tile(const JoinParams& P, uint32_t& s, 
 // skipped (warp-uniform), their accumulators stay unused.
 template <int CH>
 __device__ __forceinline__ void f32_dists(const float4* __restrict__ qrow, const float4* sA, uint32_t nq4,
-                                          uint32_t d, uint32_t na, float (&acc)[CH]) {
-  const uint32_t full = d >> 2, tail = d & 3;
+                                          uint32_t na, float (&acc)[CH]) {
+  // rows are zero padded to nq4 float4 (padding adds exact zeros); packed
+  // FP32 pairs as in k_join_f32r: even and odd coordinates summed apart
+  unsigned long long acc2[CH];
 #pragma unroll
-  for (int a = 0; a < CH; ++a) acc[a] = 0.f;
-  for (uint32_t c = 0; c < full; ++c) {
-    const float4 qq = qrow[c];
+  for (int a = 0; a < CH; ++a) acc2[a] = 0ull;
+  const ulonglong2* q2 = reinterpret_cast<const ulonglong2*>(qrow);
+  const ulonglong2* a2 = reinterpret_cast<const ulonglong2*>(sA);
+  for (uint32_t c = 0; c < nq4; ++c) {
+    const ulonglong2 qq = q2[c];
 #pragma unroll
     for (int a = 0; a < CH; ++a) {
       if (a >= (int)na) break;
-      const float4 aa = sA[a * nq4 + c];
-      float t;
-      t = aa.x - qq.x; acc[a] = fmaf(t, t, acc[a]);
-      t = aa.y - qq.y; acc[a] = fmaf(t, t, acc[a]);
-      t = aa.z - qq.z; acc[a] = fmaf(t, t, acc[a]);
-      t = aa.w - qq.w; acc[a] = fmaf(t, t, acc[a]);
+      const ulonglong2 aa = a2[a * nq4 + c];
+      unsigned long long t;
+      asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t) : "l"(aa.x), "l"(qq.x));
+      asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[a]) : "l"(t));
+      asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t) : "l"(aa.y), "l"(qq.y));
+      asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[a]) : "l"(t));
     }
   }
-  if (tail) {
-    const float4 qq = qrow[full];
 #pragma unroll
-    for (int a = 0; a < CH; ++a) {
-      if (a >= (int)na) break;
-      const float4 aa = sA[a * nq4 + full];
-      float t;
-      t = aa.x - qq.x; acc[a] = fmaf(t, t, acc[a]);
-      if (tail > 1) { t = aa.y - qq.y; acc[a] = fmaf(t, t, acc[a]); }
-      if (tail > 2) { t = aa.z - qq.z; acc[a] = fmaf(t, t, acc[a]); }
-    }
+  for (int a = 0; a < CH; ++a) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(acc2[a]));
+    acc[a] = lo + hi;
   }
 }
 
@@ -244,7 +242,7 @@ k_join_f32(const JoinParams P) {
       const uint32_t q = t.q;
       const float4* qrow = X + (size_t)(t.qv ? q : a0) * nq4;
       float acc[CH];
-      f32_dists<CH>(qrow, sA, nq4, P.d, na, acc);
+      f32_dists<CH>(qrow, sA, nq4, na, acc);
       uint32_t m = 0;
 #pragma unroll
       for (int a = 0; a < CH; ++a) {
@@ -303,33 +301,40 @@ k_join_f32r(const JoinParams P) {
     while (s < U.s1) {
       const CandTile t = next_tile(P, s, off, U.s1);
       const uint32_t q = t.q;
-      const float4* qrow = X + (size_t)(t.qv ? q : a0) * DQ;
-      float4 qq[DQ];
+      const ulonglong2* qrow = reinterpret_cast<const ulonglong2*>(X + (size_t)(t.qv ? q : a0) * DQ);
+      ulonglong2 qq[DQ];  // the candidate row as pairs of floats
 #pragma unroll
       for (int c = 0; c < DQ; ++c) qq[c] = qrow[c];
       uint32_t m = 0, lo_m = 0;
 #pragma unroll
       for (int g = 0; g < CH / 8; ++g) {
         if (g * 8 >= (int)na) break;
-        float acc[8];
+        // packed FP32 pairs (Blackwell f32x2, per-lane IEEE rounding): each
+        // home row accumulates its even and odd coordinates separately and
+        // adds the two sums at the end; the filter's error bound holds for
+        // any summation order, and half the instructions are issued
+        unsigned long long acc2[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) acc[i] = 0.f;
+        for (int i = 0; i < 8; ++i) acc2[i] = 0ull;
 #pragma unroll
         for (int c = 0; c < DQ; ++c) {
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
-            const float4 aa = sA[(g * 8 + i) * DQ + c];
-            float tt;
-            tt = aa.x - qq[c].x; acc[i] = fmaf(tt, tt, acc[i]);
-            tt = aa.y - qq[c].y; acc[i] = fmaf(tt, tt, acc[i]);
-            tt = aa.z - qq[c].z; acc[i] = fmaf(tt, tt, acc[i]);
-            tt = aa.w - qq[c].w; acc[i] = fmaf(tt, tt, acc[i]);
+            const ulonglong2 aa = reinterpret_cast<const ulonglong2*>(sA)[(g * 8 + i) * DQ + c];
+            unsigned long long tt;
+            asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(tt) : "l"(aa.x), "l"(qq[c].x));
+            asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[i]) : "l"(tt));
+            asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(tt) : "l"(aa.y), "l"(qq[c].y));
+            asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[i]) : "l"(tt));
           }
         }
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-          m |= (acc[i] <= P.t_hi ? 1u : 0u) << (g * 8 + i);
-          lo_m |= (acc[i] <= P.t_lo ? 1u : 0u) << (g * 8 + i);
+          float lo, hi;
+          asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(acc2[i]));
+          const float acc = lo + hi;
+          m |= (acc <= P.t_hi ? 1u : 0u) << (g * 8 + i);
+          lo_m |= (acc <= P.t_lo ? 1u : 0u) << (g * 8 + i);
         }
       }
       m = t.qv ? (m & home_mask(na, q >= hs && q < he, q, a0, CH)) : 0u;
