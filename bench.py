@@ -184,6 +184,24 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(ms: float, world: int, device=None) -> float:
+    """Per-step time of the job: the slowest replica's (all_reduce MAX over
+    the process group; NCCL on GPUs, gloo in the CPU tests)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_points_per_s(n_per_rank: int, world: int, ms: float) -> float:
+    """Whole-job throughput of `world` replicas that each join n_per_rank
+    points per step (weak scaling)."""
+    return world * n_per_rank / (ms * 1e-3)
+
+
 def run_reference(args, wl) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
@@ -260,11 +278,7 @@ def run_mistic(args, wl) -> None:
     e1.record(stream)
     barrier()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
     r = results[-1]
     assert all(q.pairs_ij == r.pairs_ij for q in results)
     join_ms = statistics.mean(q.ms["join"] for q in results)
@@ -282,7 +296,7 @@ def run_mistic(args, wl) -> None:
         e2e_res.append((raw.pairs_ij, raw.ms_h2d, raw.ms_d2h))
         h.lib.mistic_result_free(ctypes.byref(raw))
     barrier()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, world, dev)
 
     # ---- plain FP64 CUDA-core join on the same inputs, identical pair set
     fp64 = None
@@ -339,7 +353,7 @@ def run_mistic(args, wl) -> None:
                 "peak_source": "mistic_peaks FFMA probe, this run (CUDA-core FP32 pipe)"}
     roof["hbm_peak_gbs"] = peaks.get("hbm_gbs")
     cpu = cpu_sample(x, wl.eps, args.cpu_seconds) if not args.no_cpu else None
-    value = world * n / (ms * 1e-3)
+    value = job_points_per_s(n, world, ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -359,7 +373,7 @@ def run_mistic(args, wl) -> None:
         "k_used": r.k_used,
         "fp64_plain": fp64,
         "roofline": roof,
-        "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
+        "e2e": {"value": job_points_per_s(n, world, e2e_ms), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": n * d * x.itemsize, "d2h_bytes_per_step": int(r.pairs_ij) * 8,
                 "h2d_ms": statistics.mean(t[1] for t in e2e_res), "d2h_ms": statistics.mean(t[2] for t in e2e_res)},
         "gpu_launches": launches,
@@ -518,7 +532,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mistic", "reference"], default="mistic")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch2000"], default="susy18")
-    ap.add_argument("--n", type=int, default=0, help="override the point count (testing)")
+    ap.add_argument("--n", "--points", dest="n", type=int, default=0,
+                    help="override the point count (testing; --points under torchrun, whose parser takes --n)")
     ap.add_argument("--mode", choices=["auto", "fp32", "bf16", "fp64"], default="auto",
                     help="join mode of the timed steps")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
