@@ -534,6 +534,7 @@ def main() -> None:
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch2000"], default="susy18")
     ap.add_argument("--n", "--points", dest="n", type=int, default=0,
                     help="override the point count (testing; --points under torchrun, whose parser takes --n)")
+    ap.add_argument("--k", type=int, default=0, help="override the reference-point count (testing)")
     ap.add_argument("--mode", choices=["auto", "fp32", "bf16", "fp64"], default="auto",
                     help="join mode of the timed steps")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
@@ -549,6 +550,8 @@ def main() -> None:
             run_batch(args)
         return
     wl = WORKLOADS[args.workload][0](args.n)
+    if args.k:
+        wl.k = args.k
     if args.impl == "reference":
         run_reference(args, wl)
     else:
