@@ -331,12 +331,18 @@ def run_mistic(args, wl) -> None:
         # evaluated (home row, candidate) cell, one contraction of length d
         work = r.tc_cells * 2.0 * d
         achieved = work / (tc_ms * 1e-3) / 1e12
-        roof = {"bound": "tensor", "kernel": "k_join_tc", "achieved": achieved,
+        wide = (d + 2 + 15) // 16 * 16 > 128  # K-chunked long-row kernel
+        kname = "k_join_tcw" if wide else "k_join_tc"
+        kmma = ((d + 31) // 32 * 32) if wide else (d + 2 + 15) // 16 * 16
+        roof = {"bound": "tensor", "kernel": kname, "achieved": achieved,
                 "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
                 "frac": achieved / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
                 "traffic": None, "work": "2*d flops per evaluated cell (one d-long contraction)",
                 "peak_source": peaks["_source"] + " bf16 burst (of measured)", "kernel_ms": tc_ms,
-                "cells": r.tc_cells, "fp32_simt_peak_tflops": fp32_peak}
+                "cells": r.tc_cells, "fp32_simt_peak_tflops": fp32_peak,
+                # tensor-pipe work actually issued: 3 split products x 2 * K per
+                # 128 x 128 tile cell (padding and empty rows/columns included)
+                "issued_tflops": r.tc_tiles * 128 * 128 * 3 * 2.0 * kmma / (tc_ms * 1e-3) / 1e12}
         if args.workload == "susy18":
             roof["traffic"] = TC_DRAM_BYTES_PER_CELL_SUSY18 * r.tc_cells
             roof["traffic_source"] = ("ncu dram__bytes_read+write per cell of the 2.5M-point capture "

@@ -43,61 +43,16 @@
 
 #include "emit.cuh"
 #include "internal.cuh"
+#include "tc_common.cuh"
 
 namespace mistic {
 namespace {
 
+using namespace tcu;
+
 constexpr int TM = 128;          // home rows per tile (MMA M)
 constexpr int TN = 128;          // candidate columns per tile (MMA N)
 constexpr int WIN = 256;         // neighbour bins per candidate window
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// tcgen05 shared-memory matrix descriptor: no swizzle, K-major.
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
-  d |= (uint64_t)((128u >> 4) & 0x3FFF) << 16;  // LBO: next core matrix along K
-  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;   // SBO: next 8-row group
-  d |= (uint64_t)1 << 46;                        // descriptor version
-  return d;
-}
-
-// Instruction descriptor, kind::f16: D f32, A/B bf16, both K-major, N x M.
-__host__ __device__ constexpr uint32_t umma_idesc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-      "l"(da), "l"(db), "r"(idesc), "r"(acc));
-}
-
-// Issues one 32-column TMEM load without waiting (pair with tmem_wait).
-__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&v)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-        "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-        "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-      : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-
-
-__device__ __forceinline__ uint32_t warp_scan_incl(uint32_t x) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(FULL_MASK, x, o);
-    if (lane >= o) x += y;
-  }
-  return x;
-}
 
 // ---------------------------------------------------------------- pipeline
 // One persistent CTA per SM: 8 producer warps, NEPI epilogue warps, 1 MMA warp.
@@ -158,54 +113,7 @@ struct TcShared2 {
   unsigned long long full[NS], sfree[NS], dfull[NACC], dfree[NACC], afull, afree;
 };
 
-__device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
-}
-__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
-  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(smem_u32(b)) : "memory");
-}
-__device__ __forceinline__ void tc_commit(unsigned long long* b) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(b))
-               : "memory");
-}
 __device__ __forceinline__ void prod_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NPROD) : "memory"); }
-
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Bounded wait on an mbarrier phase.  The waiting warp is suspended by the
-// hardware (try_wait with a suspend-time hint) instead of spinning, so idle
-// roles leave the issue slots to the working ones.  After limit_ns of
-// waiting the CTA's abort flag is raised.  Returns false if the CTA is
-// aborting (now or already).
-constexpr uint32_t kSuspendNs = 20000;
-__device__ __forceinline__ bool wait_or_abort(unsigned long long* b, uint32_t parity, volatile uint32_t* abort_flag,
-                                              long long limit_ns) {
-  const uint32_t a = smem_u32(b);
-  uint32_t done;
-  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-               : "=r"(done)
-               : "r"(a), "r"(parity)
-               : "memory");
-  if (done) return true;
-  const unsigned long long t0 = global_ns();
-  for (;;) {
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(a), "r"(parity), "r"(kSuspendNs)
-        : "memory");
-    if (done) return true;
-    if (*abort_flag) return false;
-    if ((long long)(global_ns() - t0) > limit_ns) {
-      *abort_flag = 1u;
-      return false;
-    }
-  }
-}
 
 // Operand rows live in the no-swizzle K-major core-matrix layout: the
 // 16-byte chunk of row r and K block kb (8 bf16) sits at bf16 offset
@@ -214,15 +122,6 @@ __device__ __forceinline__ bool wait_or_abort(unsigned long long* b, uint32_t pa
 // block kb, [8kb+4, 8kb+8) into its lo chunk -- and then converted in place,
 // block by block, into the augmented bf16 hi/lo row.  Two threads share a
 // row, one per half of the K blocks; a thread only touches its own chunks.
-template <int KP>
-__device__ __forceinline__ uint32_t chunk_off(uint32_t r, uint32_t kb) {
-  return ((r >> 3) * (KP / 8) + kb) * 64 + (r & 7) * 8;
-}
-
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-
 template <int KP>
 __device__ __forceinline__ void load_half(__nv_bfloat16* hi, __nv_bfloat16* lo, uint32_t r, uint32_t half,
                                           const float* __restrict__ xr, uint32_t dpad) {
@@ -330,26 +229,6 @@ __device__ __forceinline__ void conv_pass2(const __nv_bfloat16* sh, const __nv_b
     }
     store_split(hi, lo, off, v);
   }
-}
-
-// Per-column threshold T(n) folded into B and the accept distance dlt(n),
-// from the unit's largest |a'|^2 and this column's |q'|^2 (FP32, rounded
-// outward).  Returns false when the bound is too wide to decide anything
-// (the column is then re-decided entirely in FP64).
-__device__ __forceinline__ bool column_threshold(const TcParams& T, float ra2max, float nq2, float* tcol,
-                                                 float* dlt) {
-  const float ra = sqrtf(ra2max * T.ginf), rq = sqrtf(nq2 * T.ginf);
-  const float rs = ra + rq;
-  const float delta = T.uR2 + T.u1 * rs;
-  const float E = (T.kappa * (rs * rs + 1.2f * T.eps2_hi) + delta * (2.f * T.Dp + delta)) * 1.001f;
-  if (!(E <= T.cap)) return false;
-  float t = T.eps2_hi + E + T.margin;
-  t += fabsf(t) * 1e-6f;
-  float dl = (T.eps2_hi - T.eps2_lo) + 2.f * E + T.margin;
-  dl += fabsf(dl) * 1e-6f;
-  *tcol = t;
-  *dlt = dl;
-  return true;
 }
 
 template <int KP, int NS, int G, int RAW, int NEPI>
@@ -938,11 +817,13 @@ namespace join {
 int tc_kp(uint32_t d) { return (int)(((d + 2) + 15) / 16 * 16); }
 // Home rows per tensor-core unit: G chunks of 128 share each converted
 // candidate tile (G = 2 while the operands leave room for two CTAs per SM).
+// Longer rows go to the K-chunked kernel (join_tcw.cu), 256 home rows a unit.
 uint32_t tc_rows(uint32_t d) {
   const int kp = tc_kp(d);
+  if (kp > 128) return 256;
   return (uint32_t)TM * (kp <= 32 ? 4 : (kp <= 64 ? 2 : 1));
 }
-bool tc_supported(uint32_t d) { return tc_kp(d) <= 128; }
+bool tc_supported(uint32_t d) { return d >= 1 && d <= MAX_D; }
 
 void run_tc(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
   if (T.n_units == 0) return;
@@ -955,7 +836,7 @@ void run_tc(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
     case 96: launch_tc<96>(h, P, T); break;
     case 112: launch_tc<112>(h, P, T); break;
     case 128: launch_tc<128>(h, P, T); break;
-    default: throw Error(MISTIC_ERR_INTERNAL, "unsupported tensor-core K");
+    default: run_tcw(h, P, T); break;
   }
 }
 

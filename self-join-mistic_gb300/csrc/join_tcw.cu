@@ -1,0 +1,600 @@
+// Tensor-core distance join for long rows (d + 2 > 128): K-chunked Gram tiles.
+//
+// Reference counterpart: the FP64 distance loop of nodeByPoint5 /
+// cachedDistanceCheck (src/kernel.cu:992-1046, 833-865).  For long rows a
+// unit -- up to 256 points of one large home bin against a segment of its
+// neighbour bins (bins >= home) -- is a dense contraction:
+//
+//   G[m][n] = a_m . q_n   (K = d, rows relative to the bounding-box centre)
+//   D'[m][n] = |a_m|^2 - 2 G[m][n] + (|q_n|^2 - T(n))
+//
+// and a pair is a candidate when D' < 0.  The sorted FP32 rows are split
+// once into bf16 hi + lo parts (k_split_rows, stored per K block of 8 as
+// [hi 16 B | lo 16 B]) with their FP32 norms; G = Ahi.Bhi + Ahi.Blo + Alo.Bhi
+// is accumulated in FP32 in tensor memory.  Unlike the short-row kernel
+// (join_tc.cu) nothing is converted inside the join: operands stream from
+// L2 into shared memory with cp.async in K chunks of 32.
+//
+// Tiles: 2 home chunks of 128 rows (MMA M = 128 each) x up to 256 candidate
+// columns (MMA N), i.e. two 128 x 256 FP32 accumulators = all 512 TMEM
+// columns.  A stage holds one K chunk of both home chunks and of the 256
+// candidate rows (64 KB); three stages are in flight.
+//
+// Exactness: the same rigorous bound as the short-row kernel (split error
+// 3.02 * 2^-18 per |a_k||q_k|, 2^-19 per MMA instruction of accumulation,
+// FP32 norms, global FP32 centring), plus the FP32 epilogue arithmetic
+// (accounted for in TcParams.kappa by the host): D' <= -dlt(n) accepts,
+// D' < 0 otherwise goes to the band list, whose pairs are re-decided with
+// the reference FP64 predicate.  Columns whose bound exceeds 0.1 eps2 are
+// re-decided entirely in FP64.
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+
+#include "emit.cuh"
+#include "internal.cuh"
+#include "tc_common.cuh"
+
+namespace mistic {
+namespace {
+
+using namespace tcu;
+
+constexpr int WM = 128;      // rows per home chunk (MMA M)
+constexpr int WG = 2;        // home chunks per unit
+constexpr int WN = 256;      // candidate columns per group (MMA N at most)
+constexpr int WKC = 32;      // K per pipeline stage (two MMA K steps of 16)
+constexpr int WNS = 3;       // stages
+constexpr int WWIN = 256;    // neighbour bins per candidate window
+constexpr int WNPW = 8;      // producer warps: thread t loads home row t and candidate row t
+constexpr int WNPROD = WNPW * 32;
+constexpr int WNEPI = 8;     // epilogue warps: 4 TMEM lane quarters x 2 column halves
+constexpr int WEPI0 = WNPW;  // first epilogue warp (a multiple of 4: warp % 4 is its lane quarter)
+constexpr int WMMA = WEPI0 + WNEPI;
+constexpr int WTHREADS = (WMMA + 1) * 32;
+constexpr int WGS = 2;       // group metadata slots
+constexpr uint32_t A_OP = WG * WM * WKC;  // bf16 per stage of the home rows (hi or lo)
+constexpr uint32_t B_OP = WN * WKC;       // bf16 per stage of the candidate rows (hi or lo)
+constexpr uint32_t STAGE_ELEMS = 2 * A_OP + 2 * B_OP;
+constexpr uint32_t WFLAG_END = 1;
+static_assert(WNPROD == WG * WM && WNPROD == WN, "one producer thread per operand row");
+
+// Everything the epilogue needs about one group (a unit's home rows x up to
+// 256 candidate columns).  Written by the producers before the group's first
+// stage is published; released by the epilogue (gfree) when it is done.
+struct __align__(16) WGroup {
+  uint32_t qid[WN];      // original ids of the candidates
+  float hq[WN];          // |q|^2 - T(n)
+  float dlt[WN];         // accept when D' <= -dlt
+  uint32_t aid[WG * WM]; // original ids of the home rows
+  float na[WG * WM];     // |a|^2 of the home rows
+  uint32_t a0, nrows, ncols, ng, flags;
+  uint32_t hlo, hhi, hq0;  // columns [hlo, hhi) are home-bin rows, column hlo at sorted position hq0
+};
+
+struct WShared {
+  WGroup grp[WGS];
+  uint32_t w_start[WWIN];
+  uint32_t w_pref[WWIN + 1];
+  uint32_t scan_ws[WNPW];
+  unsigned long long unit;
+  uint32_t w_home;   // (window generation << 8) | index of the home bin in the window
+  uint32_t ra2max;   // float bits, non-negative
+  uint32_t abort_flag;
+  uint32_t tmem_base;
+  uint32_t pflag[2];
+  unsigned long long full[WNS], sfree[WNS], dfull[WG], dfree[WG], gfree[WGS];
+};
+
+__device__ __forceinline__ void wprod_sync() { asm volatile("bar.sync 1, %0;" ::"n"(WNPROD) : "memory"); }
+
+__device__ __forceinline__ void cp_async16_ca(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+// One warp per sorted row: bf16 hi/lo split of the FP32 row (zero beyond its
+// dpad32 stored values, up to kd) and its FP32 squared norm.  Output row layout: kd / 8 blocks of
+// [hi: 8 bf16 | lo: 8 bf16].
+__global__ void k_split_rows(const float* __restrict__ xf, uint32_t dpad32, uint32_t kd, size_t n,
+                             uint4* __restrict__ xw, float* __restrict__ xn) {
+  const size_t row = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float* x = xf + row * dpad32;
+  uint4* out = xw + row * (kd / 8) * 2;
+  float acc = 0.f;
+  for (uint32_t kb = lane; kb < kd / 8; kb += 32) {
+    float v[8];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint32_t k0 = kb * 8 + 4 * h;
+      float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (k0 < dpad32) f = *reinterpret_cast<const float4*>(x + k0);  // dpad32 % 4 == 0, zero beyond d
+      v[4 * h] = f.x, v[4 * h + 1] = f.y, v[4 * h + 2] = f.z, v[4 * h + 3] = f.w;
+    }
+    uint4 oh, ol;
+    uint32_t* ph = reinterpret_cast<uint32_t*>(&oh);
+    uint32_t* pl = reinterpret_cast<uint32_t*>(&ol);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      acc = fmaf(v[2 * i], v[2 * i], acc);
+      acc = fmaf(v[2 * i + 1], v[2 * i + 1], acc);
+      const __nv_bfloat162 hv = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+      const float2 hf = __bfloat1622float2(hv);
+      const __nv_bfloat162 lv = __floats2bfloat162_rn(v[2 * i] - hf.x, v[2 * i + 1] - hf.y);
+      ph[i] = *reinterpret_cast<const uint32_t*>(&hv);
+      pl[i] = *reinterpret_cast<const uint32_t*>(&lv);
+    }
+    out[2 * kb] = oh;
+    out[2 * kb + 1] = ol;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(FULL_MASK, acc, o);
+  if (lane == 0) xn[row] = acc;
+}
+
+// ---------------------------------------------------------------- pipeline
+// One persistent CTA per SM: 8 producer warps, 8 epilogue warps, 1 MMA warp.
+//   producers  fetch units; per group of up to 256 candidates compute the
+//              columns' ids, norms and thresholds, then for each K chunk
+//              copy the chunk of the home rows (thread t: row t) and of the
+//              candidate rows (thread t: column t) into the next stage with
+//              cp.async; a stage is published (full) once its copies have
+//              landed, one stage behind the newest issued one;
+//   MMA warp   one lane issues 2 x 3 tcgen05.mma (K 16, M 128, N up to 256)
+//              per home chunk and stage, commits each stage to sfree and, at
+//              a group's last stage, each accumulator to dfull;
+//   epilogue   tcgen05.ld of TMEM lane quarter w % 4, D' = |a|^2 - 2G + hq,
+//              sign-bit test, home-bin rule by column range, sure accepts
+//              to the pair list, the error band to the band list.
+// Barriers (all waits bounded by a %globaltimer deadline):
+//   full[s]   producers -> MMA       (WNPROD arrivals)
+//   sfree[s]  MMA -> producers       (tcgen05.commit: stage s read)
+//   dfull[g]  MMA -> epilogue        (tcgen05.commit, or a plain arrive to stop)
+//   dfree[g]  epilogue -> MMA        (WNEPI arrivals; accumulator g reusable)
+//   gfree[x]  epilogue -> producers  (WNEPI arrivals; group slot x reusable)
+__global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, const TcParams T) {
+  extern __shared__ __align__(128) unsigned char tcw_dyn[];
+  __shared__ WShared S;
+  __nv_bfloat16* stages = reinterpret_cast<__nv_bfloat16*>(tcw_dyn);  // WNS x [Ahi | Alo | Bhi | Blo]
+  unsigned long long* pstage = reinterpret_cast<unsigned long long*>(stages + WNS * STAGE_ELEMS);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint4* XW = T.xw;
+  const uint32_t kb_row = T.kd / 8;  // K blocks per row
+  const uint32_t nkc = T.kd / WKC;   // stages per group
+  volatile uint32_t* abort_flag = &S.abort_flag;
+
+  if (tid == 0) {
+    for (int i = 0; i < WNS; ++i) {
+      mbar_init(&S.full[i], WNPROD);
+      mbar_init(&S.sfree[i], 1);
+    }
+    for (int i = 0; i < WG; ++i) {
+      mbar_init(&S.dfull[i], 1);
+      mbar_init(&S.dfree[i], WNEPI);
+    }
+    for (int i = 0; i < WGS; ++i) mbar_init(&S.gfree[i], WNEPI);
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    S.abort_flag = 0;
+    S.w_home = 0xffffffffu;
+  }
+  if (warp == WMMA) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&S.tmem_base)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tbase = S.tmem_base;
+
+  if (warp < WNPW) {
+    // ============================ producers
+    // Every branch that leads to bar.sync is taken on a value all producer
+    // threads hold in registers or read from shared memory after the same
+    // bar.sync; barrier waits are done by thread 0 and broadcast through
+    // S.pflag[2] (a thread is at most one bar.sync behind thread 0).
+    const uint32_t t = (uint32_t)tid;
+    uint32_t step = 0, pub = 0, group = 0, pf = 0, wgen = 0;
+    unsigned long long n_tiles = 0, n_cells = 0;
+    bool aborted = false;
+    // thread 0 waits on b (bounded), all producers learn the outcome
+    auto shared_wait = [&](unsigned long long* b, uint32_t parity) -> bool {
+      const uint32_t sl = pf++ & 1;
+      if (tid == 0) S.pflag[sl] = wait_or_abort(b, parity, abort_flag, T.wait_limit) ? 1u : 0u;
+      wprod_sync();
+      return S.pflag[sl] != 0u;
+    };
+    // publishes every issued stage but the newest `keep` once its copies landed
+    auto publish = [&](uint32_t keep) {
+      while (pub + keep < step) {
+        if (step - pub > 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
+        else asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(&S.full[pub % WNS]);
+        ++pub;
+      }
+    };
+    for (;;) {
+      const uint32_t slot = pf++ & 1;
+      if (tid == 0) {
+        const unsigned long long uu = atomicAdd(&T.ctr->next_unit, 1ull);
+        S.unit = uu;
+        S.ra2max = 0;
+        S.pflag[slot] = (uu < T.n_units && !*abort_flag) ? 1u : 0u;
+      }
+      wprod_sync();
+      if (!S.pflag[slot]) break;
+      const Unit U = T.units[S.unit];
+      const uint32_t hs = P.bstart[U.h], he = P.bstart[U.h + 1];
+      const uint32_t a0 = hs + U.chunk * (WG * WM);
+      const uint32_t nrows = min((uint32_t)(WG * WM), he - a0);
+      const uint32_t ng = (nrows + WM - 1) / WM;
+      const bool arow = t < nrows;
+      const uint32_t my_aid = arow ? P.ids[a0 + t] : 0u;
+      const float my_na = arow ? T.xn[a0 + t] : 0.f;
+      {
+        float m = my_na;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL_MASK, m, o));
+        if (lane == 0) atomicMax(&S.ra2max, __float_as_uint(m));
+      }
+      wprod_sync();
+      const float ra2max = __uint_as_float(S.ra2max);
+      const uint4* arow_src = XW + (size_t)(a0 + t) * kb_row * 2;
+
+      uint32_t seg_next = U.s0, w_nb = 0, w_pos = 0, w_total = 0;
+      int w_hj = -1;
+      while (w_pos < w_total || seg_next < U.s1) {
+        if (w_pos >= w_total) {  // next window of up to WWIN neighbour bins
+          const uint32_t nb = min((uint32_t)WWIN, U.s1 - seg_next);
+          uint32_t st0 = 0, sz0 = 0, bn = 0xffffffffu;
+          if (t < nb) {
+            bn = P.nbr[seg_next + t];
+            st0 = P.bstart[bn];
+            sz0 = P.bstart[bn + 1] - st0;
+          }
+          const uint32_t incl = warp_scan_incl(sz0);
+          if (lane == 31) S.scan_ws[warp] = incl;
+          wprod_sync();
+          uint32_t wp = 0;
+          for (int w = 0; w < warp; ++w) wp += S.scan_ws[w];
+          ++wgen;
+          if (t < nb) {
+            S.w_start[t] = st0;
+            S.w_pref[t + 1] = wp + incl;
+            if (bn == U.h) S.w_home = ((wgen & 0xffffffu) << 8) | t;
+          }
+          if (tid == 0) S.w_pref[0] = 0;
+          wprod_sync();
+          {
+            const uint32_t wh = S.w_home;
+            w_hj = (wh >> 8) == (wgen & 0xffffffu) ? (int)(wh & 255u) : -1;
+          }
+          w_nb = nb;
+          w_pos = 0;
+          w_total = S.w_pref[nb];
+          seg_next += nb;
+        }
+        // ---- a group: columns [w_pos, w_pos + ncols) of the window
+        const uint32_t ncols = min((uint32_t)WN, w_total - w_pos);
+        const bool bcol = t < ncols;
+        uint32_t q = 0;
+        if (bcol) {
+          const uint32_t rank = w_pos + t;
+          int lo = 0, hi = (int)w_nb - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (S.w_pref[mid] <= rank) lo = mid; else hi = mid - 1;
+          }
+          q = S.w_start[lo] + (rank - S.w_pref[lo]);
+        }
+        float hqv = 0.f, dl = 0.f;
+        uint32_t qid = 0;
+        if (bcol) {
+          qid = P.ids[q];
+          const float nq2 = T.xn[q];
+          float tcol;
+          if (column_threshold(T, ra2max, nq2, &tcol, &dl)) {
+            hqv = nq2 - tcol;
+          } else {
+            hqv = -1e30f;   // every row of this column becomes a candidate ...
+            dl = INFINITY;  // ... and none is accepted without the FP64 check
+          }
+        }
+        const uint32_t gs = group % WGS;
+        if (!shared_wait(&S.gfree[gs], ((group / WGS) & 1) ^ 1)) {
+          aborted = true;
+          break;
+        }
+        WGroup& Gm = S.grp[gs];
+        Gm.qid[t] = qid;
+        Gm.hq[t] = hqv;
+        Gm.dlt[t] = dl;
+        Gm.aid[t] = my_aid;
+        Gm.na[t] = my_na;
+        if (tid == 0) {
+          uint32_t hlo = 0, hhi = 0, hq0 = 0;
+          if (w_hj >= 0) {
+            const uint32_t hr0 = S.w_pref[w_hj], hr1 = S.w_pref[w_hj + 1];
+            const uint32_t lo = max(hr0, w_pos), hi = min(hr1, w_pos + ncols);
+            if (lo < hi) {
+              hlo = lo - w_pos;
+              hhi = hi - w_pos;
+              hq0 = hs + (lo - hr0);
+            }
+          }
+          Gm.a0 = a0;
+          Gm.nrows = nrows;
+          Gm.ncols = ncols;
+          Gm.ng = ng;
+          Gm.flags = 0;
+          Gm.hlo = hlo;
+          Gm.hhi = hhi;
+          Gm.hq0 = hq0;
+          n_tiles += (unsigned long long)ng * ((ncols + 127) / 128);
+          n_cells += (unsigned long long)nrows * ncols;
+        }
+        const uint4* bsrc = XW + (size_t)q * kb_row * 2;
+        for (uint32_t kc = 0; kc < nkc; ++kc) {
+          const uint32_t s = step % WNS;
+          if (!shared_wait(&S.sfree[s], ((step / WNS) & 1) ^ 1)) {
+            aborted = true;
+            break;
+          }
+          __nv_bfloat16* st = stages + s * STAGE_ELEMS;
+          __nv_bfloat16 *ahi = st, *alo = st + A_OP, *bhi = st + 2 * A_OP, *blo = bhi + B_OP;
+#pragma unroll
+          for (int j = 0; j < WKC / 8; ++j) {
+            const uint32_t gkb = kc * (WKC / 8) + j;  // K block within the row
+            const uint32_t off = chunk_off<WKC>(t, j);
+            if (arow) {
+              cp_async16_ca(ahi + off, arow_src + 2 * gkb);
+              cp_async16_ca(alo + off, arow_src + 2 * gkb + 1);
+            }
+            if (bcol) {
+              cp_async16_ca(bhi + off, bsrc + 2 * gkb);
+              cp_async16_ca(blo + off, bsrc + 2 * gkb + 1);
+            }
+          }
+          asm volatile("cp.async.commit_group;" ::: "memory");
+          ++step;
+          publish(1);
+        }
+        if (aborted) break;
+        w_pos += ncols;
+        ++group;
+      }
+      if (aborted) break;
+    }
+    if (!aborted) {
+      publish(0);
+      // stop marker: a group slot flagged END behind a stage with no copies
+      const uint32_t gs = group % WGS, s = step % WNS;
+      bool ok = shared_wait(&S.gfree[gs], ((group / WGS) & 1) ^ 1);
+      if (ok) ok = shared_wait(&S.sfree[s], ((step / WNS) & 1) ^ 1);
+      if (ok) {
+        if (tid == 0) S.grp[gs].flags = WFLAG_END;
+        wprod_sync();
+        mbar_arrive(&S.full[s]);
+      }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    if (tid == 0 && n_tiles) {
+      atomicAdd(&T.ctr->tiles, n_tiles);
+      atomicAdd(&T.ctr->cells, n_cells);
+    }
+  } else if (warp == WMMA) {
+    // ============================ MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t SBO = 16u * WKC;
+      uint32_t step = 0, group = 0;
+      uint32_t use[WG] = {0, 0};
+      unsigned long long* last_bar = nullptr;
+      uint32_t last_par = 0;
+      bool ok = true;
+      while (ok) {
+        uint32_t s = step % WNS;
+        ok = wait_or_abort(&S.full[s], (step / WNS) & 1, abort_flag, T.wait_limit);
+        if (!ok) break;
+        const WGroup& Gm = S.grp[group % WGS];
+        if (Gm.flags & WFLAG_END) {
+          mbar_arrive(&S.dfull[0]);
+          break;
+        }
+        const uint32_t ng = Gm.ng;
+        const uint32_t nmma = max(16u, (Gm.ncols + 15u) & ~15u);  // MMA N: the group's columns, rounded to 16
+        const uint32_t idesc = umma_idesc(WM, (int)nmma);
+        for (uint32_t kc = 0; kc < nkc && ok; ++kc) {
+          if (kc > 0) {
+            s = step % WNS;
+            ok = wait_or_abort(&S.full[s], (step / WNS) & 1, abort_flag, T.wait_limit);
+            if (!ok) break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const __nv_bfloat16* st = stages + s * STAGE_ELEMS;
+          const uint32_t bh = smem_u32(st + 2 * A_OP), bl = smem_u32(st + 2 * A_OP + B_OP);
+          for (uint32_t g = 0; g < ng; ++g) {
+            if (kc == 0) {  // first writes of this group into accumulator g
+              ok = wait_or_abort(&S.dfree[g], (use[g] & 1) ^ 1, abort_flag, T.wait_limit);
+              if (!ok) break;
+              asm volatile("tcgen05.fence::after_thread_sync;");
+            }
+            const uint32_t ah = smem_u32(st + g * WM * WKC), al = smem_u32(st + A_OP + g * WM * WKC);
+            const uint32_t dt = tbase + g * WN;
+#pragma unroll
+            for (int ks = 0; ks < WKC / 16; ++ks) {
+              const uint32_t o = ks * 256;  // two K blocks of 128 B
+              mma_bf16(dt, umma_desc(ah + o, SBO), umma_desc(bh + o, SBO), idesc, (kc | ks) ? 1u : 0u);
+              mma_bf16(dt, umma_desc(ah + o, SBO), umma_desc(bl + o, SBO), idesc, 1u);
+              mma_bf16(dt, umma_desc(al + o, SBO), umma_desc(bh + o, SBO), idesc, 1u);
+            }
+          }
+          if (!ok) break;
+          tc_commit(&S.sfree[s]);  // the stage may be refilled once these MMAs have read it
+          last_bar = &S.sfree[s];
+          last_par = (step / WNS) & 1;
+          ++step;
+        }
+        if (!ok) break;
+        for (uint32_t g = 0; g < ng; ++g) {
+          tc_commit(&S.dfull[g]);
+          last_bar = &S.dfull[g];
+          last_par = use[g] & 1;
+          ++use[g];
+        }
+        ++group;
+      }
+      // an aborting CTA may still have MMAs in flight: wait (bounded) for the
+      // last commit, MMAs complete in issue order
+      if (*abort_flag && last_bar) {
+        volatile uint32_t no_abort = 0;
+        wait_or_abort(last_bar, last_par, &no_abort, T.wait_limit);
+      }
+    }
+    __syncwarp();
+  } else if (warp >= WEPI0 && warp < WEPI0 + WNEPI) {
+    // ============================ epilogue
+    // warp w reads TMEM lane quarter w % 4 (the hardware's access rule) and
+    // the 32-column blocks (w - WEPI0) / 4, + 2, + 4, ... of each accumulator
+    const uint32_t quarter = warp & 3;
+    const uint32_t cblk0 = (warp - WEPI0) >> 2;
+    PairStage ps{pstage + (warp - WEPI0) * PSTAGE, 0};
+    PairStage bs{pstage + (WNEPI + warp - WEPI0) * PSTAGE, 0};
+    uint32_t group = 0;
+    uint32_t use[WG] = {0, 0};
+    bool run = true;
+    while (run) {
+      const uint32_t gs = group % WGS;
+      const WGroup& Gm = S.grp[gs];
+      uint32_t ng = 1;
+      for (uint32_t g = 0; g < ng; ++g) {
+        // all lanes wait; the outcome is made warp-uniform (tcgen05.ld is .sync.aligned)
+        const bool ok = __all_sync(FULL_MASK, wait_or_abort(&S.dfull[g], use[g] & 1, abort_flag, T.wait_limit));
+        if (!ok || __any_sync(FULL_MASK, (Gm.flags & WFLAG_END) || *abort_flag)) {
+          run = false;
+          break;
+        }
+        if (g == 0) ng = Gm.ng;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t ncols = Gm.ncols, nrows = Gm.nrows;
+        const uint32_t row = g * WM + quarter * 32 + lane;  // row within the unit
+        const bool row_ok = row < nrows;
+        const uint32_t a_sorted = Gm.a0 + row;
+        const float na = row_ok ? Gm.na[row] : 0.f;
+        const uint32_t hlo = Gm.hlo, hhi = Gm.hhi, hq0 = Gm.hq0;
+        // columns c in [hlo, lim) hold home rows q <= a (dropped: each pair once, no self pair)
+        const uint32_t lim = (hlo < hhi && a_sorted >= hq0) ? min(hhi, hlo + min(a_sorted - hq0 + 1, (uint32_t)WN)) : 0u;
+        if (g * WM + quarter * 32 < nrows) {
+#pragma unroll 1
+          for (uint32_t c0 = 32 * cblk0; c0 < ncols; c0 += 32 * (WNEPI / 4)) {
+            uint32_t v[32];
+            tmem_ld32_nowait(tbase + g * WN + ((quarter * 32u) << 16) + c0, v);
+            tmem_wait();
+            uint32_t o = 0;
+#pragma unroll
+            for (int j = 0; j < 32; j += 4) {
+              const float4 h4 = *reinterpret_cast<const float4*>(&Gm.hq[c0 + j]);
+              const float hv[4] = {h4.x, h4.y, h4.z, h4.w};
+#pragma unroll
+              for (int i = 0; i < 4; ++i) {
+                const float dv = fmaf(-2.f, __uint_as_float(v[j + i]), na) + hv[i];
+                v[j + i] = __float_as_uint(dv);
+                o |= v[j + i];
+              }
+            }
+            uint32_t acc_bits = 0, band_bits = 0;
+            const uint32_t nvalid = min(32u, ncols - c0);
+            const bool maybe = row_ok && (o >> 31);
+            if (__any_sync(FULL_MASK, maybe)) {
+              if (maybe) {
+                uint32_t m = 0;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) m |= (v[j] >> 31) << j;
+                m &= nvalid >= 32 ? FULL_MASK : ((1u << nvalid) - 1u);
+                const int e0 = (int)max(hlo, c0) - (int)c0, e1 = (int)min(lim, c0 + 32) - (int)c0;
+                if (e0 < e1) m &= ~((e1 >= 32 ? FULL_MASK : ((1u << e1) - 1u)) & ~((1u << e0) - 1u));
+                while (m) {
+                  const int j = __ffs(m) - 1;
+                  m &= m - 1;
+                  if (pick32(v, j) <= -Gm.dlt[c0 + j])
+                    acc_bits |= 1u << j;
+                  else
+                    band_bits |= 1u << j;  // decided later in FP64 (band list)
+                }
+              }
+            }
+            __syncwarp();
+            const uint32_t ia = (acc_bits | band_bits) ? Gm.aid[row] : 0u;
+            auto emit = [&](PairStage& stg, uint32_t bits, unsigned long long* counter, unsigned long long* list,
+                            unsigned long long lcap) {
+              stage_pairs(
+                  stg, __popc(bits),
+                  [&](uint32_t) {
+                    const int j = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    const uint32_t iq = Gm.qid[c0 + j];
+                    const uint32_t lo = ia < iq ? ia : iq, hi = ia < iq ? iq : ia;
+                    return ((unsigned long long)lo << 32) | hi;
+                  },
+                  counter, list, lcap);
+            };
+            if (__any_sync(FULL_MASK, acc_bits != 0u)) emit(ps, acc_bits, &P.ctr->pairs, P.pairs, P.cap);
+            if (__any_sync(FULL_MASK, band_bits != 0u)) emit(bs, band_bits, &P.ctr->band_n, P.band_list, P.band_cap);
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&S.dfree[g]);
+        ++use[g];
+      }
+      if (!run) break;
+      if (lane == 0) mbar_arrive(&S.gfree[gs]);
+      ++group;
+    }
+    stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
+    stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap);
+  }
+  // all roles meet here before tensor memory is released
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == WMMA) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tbase));
+  if (tid == 0 && S.abort_flag) atomicExch(&P.ctr->error, 1ull);
+}
+
+}  // namespace
+
+namespace join {
+
+uint32_t tcw_kd(uint32_t d) { return (d + WKC - 1) / WKC * WKC; }
+
+void tcw_prepare(mistic_handle_s* h, const float* xf, uint32_t dpad32, uint32_t d, size_t n, uint4* xw, float* xn) {
+  if (n == 0) return;
+  const unsigned rows_per_block = 8;
+  const unsigned grid = (unsigned)((n + rows_per_block - 1) / rows_per_block);
+  k_split_rows<<<grid, rows_per_block * 32, 0, h->stream>>>(xf, dpad32, tcw_kd(d), n, xw, xn);
+  launched(h, "split_rows");
+}
+
+void run_tcw(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
+  if (T.n_units == 0) return;
+  if (!T.xw || !T.xn || T.kd % WKC) throw Error(MISTIC_ERR_INTERNAL, "long-row tensor-core join without split rows");
+  const size_t dyn = (size_t)WNS * STAGE_ELEMS * sizeof(__nv_bfloat16) +
+                     (size_t)2 * WNEPI * PSTAGE * sizeof(unsigned long long);
+  MCK(cudaFuncSetAttribute(k_join_tcw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  MCK(cudaFuncSetAttribute(k_join_tcw, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  int per_sm = 0;
+  MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join_tcw, WTHREADS, dyn));
+  if (per_sm < 1) throw Error(MISTIC_ERR_TOO_LARGE, "long-row tensor-core join does not fit on an SM");
+  const unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)h->sms, T.n_units);
+  if (getenv("MISTIC_DEBUG"))
+    fprintf(stderr, "[mistic] join_tcw KD=%u dyn=%zu occupancy=%d grid=%u units=%llu\n", T.kd, dyn, per_sm, grid,
+            (unsigned long long)T.n_units);
+  k_join_tcw<<<grid, WTHREADS, dyn, h->stream>>>(P, T);
+  launched(h, "join_tcw");
+}
+
+}  // namespace join
+}  // namespace mistic

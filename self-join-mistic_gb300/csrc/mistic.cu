@@ -256,6 +256,10 @@ int bit_length(uint64_t v) {
 uint32_t tc_min_bin(uint32_t d) {
   const char* e = getenv("MISTIC_TC_MIN_BIN");
   if (e && *e) return (uint32_t)std::max(1l, strtol(e, nullptr, 10));
+  // long rows (K-chunked kernel): a tile costs ~3 * 2 * 128 * d tensor flops
+  // per candidate column whatever its home rows, the FP32 CUDA cores 3 d
+  // per row and column, so bins of fewer than ~16 rows stay on the CUDA cores
+  if (join::tc_kp(d) > 128) return 16;
   return (uint32_t)std::min(64.0, std::max(1.0, std::floor(20000.0 / ((double)d * d))));
 }
 
@@ -552,7 +556,10 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     const double u = ldexp(1.0, -24) * (1.0 + ldexp(1.0, -20));
     const double gd = d * u / (1.0 - d * u);
     const double g64 = (d + 2) * ldexp(1.0, -53) * 1.01;
-    const int n_mma = 3 * join::tc_kp(d) / 16;
+    // long rows (augmented K above one 128-wide operand tile) use the
+    // K-chunked kernel over rows split once into bf16 hi/lo
+    const bool wide = join::tc_kp(d) > 128;
+    const int n_mma = 3 * (wide ? (int)join::tcw_kd(d) : join::tc_kp(d)) / 16;
     tp.units = units_tc;
     tp.n_units = tots[2];
     tp.ctr = ctr + 1;
@@ -562,7 +569,10 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     if ((double)tp.eps2_hi < eps2 / (1.0 - g64)) tp.eps2_hi = nextafterf(tp.eps2_hi, INFINITY);
     // split error + MMA accumulation (2^-19 per instruction) + FP32 norms +
     // rounding of the folded column |q'|^2 - T, per (|a'| + |q'|)^2 + 1.2 eps2
-    tp.kappa = (float)(((3.02 * ldexp(1.0, -18) + n_mma * 1.01 * ldexp(1.0, -19)) * (1.0 + gd) + gd + u) * 1.01);
+    // (the long-row kernel forms D' = |a|^2 - 2G + (|q|^2 - T) in FP32: three
+    // roundings, each within u (|a| + |q|)^2 + u T, instead of the folded column)
+    tp.kappa = (float)(((3.02 * ldexp(1.0, -18) + n_mma * 1.01 * ldexp(1.0, -19)) * (1.0 + gd) + gd +
+                        (wide ? 5.0 : 1.0) * u) * 1.01);
     tp.ginf = (float)(1.0 / (1.0 - gd) * (1.0 + 1e-6));
     tp.uR2 = (float)(2.0 * u * R * 1.0001);
     tp.u1 = (float)(u * (1.0 + u) * 1.0001);
@@ -576,6 +586,14 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     tp.stall_test = (st && *st == '1') ? 1 : 0;
     tp.wait_limit = tp.stall_test ? 2000000ll : 2000000000ll;  // 2 ms in the test, else 2 s
     tp.prof = getenv("MISTIC_DEBUG") ? 1 : 0;
+    if (wide && tots[2] > 0) {
+      tp.kd = join::tcw_kd(d);
+      uint4* xw = abuf<uint4>(h, "xw", n * (size_t)(tp.kd / 8) * 2);
+      float* xn = abuf<float>(h, "xn", n);
+      join::tcw_prepare(h, xf, dpad32, d, n, xw, xn);
+      tp.xw = xw;
+      tp.xn = xn;
+    }
   }
   const bool want_pairs = o.pairs != MISTIC_PAIRS_NONE;
   const bool want_csr = o.csr != MISTIC_PAIRS_NONE;
