@@ -298,27 +298,66 @@ def run_mistic(args, wl) -> None:
     barrier()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, world, dev)
 
-    # ---- plain FP64 CUDA-core join on the same inputs, identical pair set
+    # ---- full-size check: neighbour counts of sampled row blocks from the
+    # GPU FP64 brute force (mistic_bruteforce_rows) against the degrees of
+    # the timed run's pair list
+    verify = None
+    if args.verify_rows > 0:
+        pr = pbuf[:r.pairs_ij]
+        deg = torch.zeros(n, dtype=torch.int64, device=dev)
+        ones = torch.ones(pr.numel(), dtype=torch.int64, device=dev)
+        deg.index_add_(0, (pr >> 32) & 0xFFFFFFFF, ones)  # packed (i << 32 | j) or (j << 32 | i)
+        deg.index_add_(0, pr & 0xFFFFFFFF, ones)
+        half = max(1, args.verify_rows // 2)
+        lo0 = int(np.random.default_rng(7).integers(0, max(1, n - half)))
+        ok = True
+        for lo in (lo0, max(0, n - half)):
+            hi = min(n, lo + half)
+            bf = h.bruteforce_rows(None, wl.eps, lo, hi, on_device_ptr=xt.data_ptr(), n=n, d=d, dtype=dt)
+            ok = ok and bool(np.array_equal(bf.astype(np.int64), deg[lo:hi].cpu().numpy()))
+        verify = {"rows": 2 * half, "degrees_match": ok,
+                  "source": "GPU FP64 brute force over two row blocks (mistic_bruteforce_rows)"}
+
+    # ---- plain FP64 CUDA-core join on the same inputs (or on the first
+    # --fp64-rows rows, where the full plain join would take hours), identical pair set
     fp64 = None
     if not args.no_fp64:
-        pb2 = torch.empty_like(pbuf)
-        o_s = h.opts(input_on_device=True, pairs="device", pair_capacity=cap, pair_buffer=pbuf.data_ptr(),
+        m = n if args.fp64_rows <= 0 else min(n, args.fp64_rows)
+        rm = h.to_result(h.selfjoin_raw(xt.data_ptr(), m, d, dt, wl.k, wl.eps,
+                                        h.opts(input_on_device=True, mode=args.mode)))
+        capm = int(rm.pairs_ij * 1.02) + 1024
+        pa = torch.empty((capm,), dtype=torch.int64, device=dev)
+        pb2 = torch.empty_like(pa)
+        o_s = h.opts(input_on_device=True, pairs="device", pair_capacity=capm, pair_buffer=pa.data_ptr(),
                      sort_pairs=True, mode=args.mode)
-        o_f = h.opts(input_on_device=True, pairs="device", pair_capacity=cap, pair_buffer=pb2.data_ptr(),
+        o_f = h.opts(input_on_device=True, pairs="device", pair_capacity=capm, pair_buffer=pb2.data_ptr(),
                      sort_pairs=True, mode="fp64")
-        rs = step(o_s)
+
+        def step_m(opts):
+            return h.to_result(h.selfjoin_raw(xt.data_ptr(), m, d, dt, wl.k, wl.eps, opts))
+
         barrier()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        rs = step_m(o_s)
+        s1.record(stream)
+        barrier()
+        mms = s0.elapsed_time(s1) if m < n else ms
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record(stream)
-        rf = step(o_f)
+        rf = step_m(o_f)
         f1.record(stream)
         barrier()
         fms = f0.elapsed_time(f1)
         same = (rs.pairs_ij == rf.pairs_ij and
-                bool(torch.equal(pbuf[:rs.pairs_ij], pb2[:rf.pairs_ij])))
+                bool(torch.equal(pa[:rs.pairs_ij], pb2[:rf.pairs_ij])))
         fp64 = {"ms_per_step": fms, "join_ms": rf.ms["join"], "pairs_ij": rf.pairs_ij,
-                "identical_pair_set": same, "mixed_speedup": fms / ms,
+                "identical_pair_set": same, "mixed_speedup": fms / mms,
                 "ulp_ambiguous": rf.ulp_ambiguous}
+        if m < n:
+            fp64.update({"rows": m, "mixed_ms_same_rows": mms,
+                         "note": f"plain FP64 and mixed precision both timed on the first {m} rows of the "
+                                 "workload (same k and eps); the full-size plain FP64 join is too long to time"})
 
     if rank != 0:
         return
@@ -378,6 +417,7 @@ def run_mistic(args, wl) -> None:
         "tc_tiles": r.tc_tiles, "tc_fill": r.tc_cells / max(1, r.tc_tiles * 128 * 128),
         "k_used": r.k_used,
         "fp64_plain": fp64,
+        "verify": verify,
         "roofline": roof,
         "e2e": {"value": job_points_per_s(n, world, e2e_ms), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": n * d * x.itemsize, "d2h_bytes_per_step": int(r.pairs_ij) * 8,
@@ -544,6 +584,10 @@ def main() -> None:
     ap.add_argument("--mode", choices=["auto", "fp32", "bf16", "fp64"], default="auto",
                     help="join mode of the timed steps")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--fp64-rows", type=int, default=0,
+                    help="time the plain FP64 comparison on the first N rows only (0: all rows)")
+    ap.add_argument("--verify-rows", type=int, default=0,
+                    help="check the neighbour counts of this many rows against the GPU FP64 brute force")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=6.0)

@@ -144,9 +144,11 @@ struct TcParams {
   int stall_test;          // failure-detection test: the MMA warp never signals (waits run out)
   int prof;                // record per-role wait/total cycles into ctr->prof (diagnostics)
   // long-row kernel (join_tcw.cu) only: split sorted rows and their norms
-  const uint4* xw;         // per row kd / 8 blocks of [hi 8 bf16 | lo 8 bf16]
+  const void* xh;          // bf16 hi parts, n_rows x kd, row-major
+  const void* xl;          // bf16 lo parts, same layout
   const float* xn;         // FP32 |x|^2 of the sorted rows
   uint32_t kd;             // d rounded up to the K chunk
+  uint64_t n_rows;         // rows of xh / xl
 };
 
 struct Timer {
@@ -238,9 +240,10 @@ int tc_kp(uint32_t d);
 uint32_t tc_rows(uint32_t d);
 void run_tc(mistic_handle_s*, const JoinParams&, const TcParams&);
 // Long rows (tc_kp(d) > 128): K-chunked kernel over rows split once into
-// bf16 hi/lo (tcw_prepare: xw holds n * tcw_kd(d) / 8 * 2 uint4, xn n floats).
+// bf16 hi/lo (tcw_prepare: xh and xl hold n x tcw_kd(d) bf16 each, xn n floats).
 uint32_t tcw_kd(uint32_t d);
-void tcw_prepare(mistic_handle_s*, const float* xf, uint32_t dpad32, uint32_t d, size_t n, uint4* xw, float* xn);
+void tcw_prepare(mistic_handle_s*, const float* xf, uint32_t dpad32, uint32_t d, size_t n, void* xh, void* xl,
+                 float* xn);
 void run_tcw(mistic_handle_s*, const JoinParams&, const TcParams&);
 }  // namespace join
 

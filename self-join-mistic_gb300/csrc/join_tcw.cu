@@ -9,11 +9,15 @@
 //   D'[m][n] = |a_m|^2 - 2 G[m][n] + (|q_n|^2 - T(n))
 //
 // and a pair is a candidate when D' < 0.  The sorted FP32 rows are split
-// once into bf16 hi + lo parts (k_split_rows, stored per K block of 8 as
-// [hi 16 B | lo 16 B]) with their FP32 norms; G = Ahi.Bhi + Ahi.Blo + Alo.Bhi
-// is accumulated in FP32 in tensor memory.  Unlike the short-row kernel
-// (join_tc.cu) nothing is converted inside the join: operands stream from
-// L2 into shared memory with cp.async in K chunks of 32.
+// once into bf16 hi and lo arrays (k_split_rows) with their FP32 norms;
+// G = Ahi.Bhi + Ahi.Blo + Alo.Bhi is accumulated in FP32 in tensor memory.
+// Unlike the short-row kernel (join_tc.cu) nothing is converted inside the
+// join: operands stream from L2 into shared memory in K chunks of 32.  The
+// home rows (contiguous) come as 128-row TMA tiles (cp.async.bulk.tensor,
+// 64-byte rows, 64B swizzle); the candidate rows, which come from several
+// bins, by cp.async in 16-byte chunks into no-swizzle core matrices.  (TMA
+// 4-row gathers of the candidate rows were measured slower: 64-byte rows
+// keep the copy engine busy far longer than the MMAs take.)
 //
 // Tiles: 2 home chunks of 128 rows (MMA M = 128 each) x up to 256 candidate
 // columns (MMA N), i.e. two 128 x 256 FP32 accumulators = all 512 TMEM
@@ -27,10 +31,13 @@
 // D' < 0 otherwise goes to the band list, whose pairs are re-decided with
 // the reference FP64 predicate.  Columns whose bound exceeds 0.1 eps2 are
 // re-decided entirely in FP64.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <math.h>
 
 #include <algorithm>
+#include <mutex>
 #include <cstdio>
 #include <cstdlib>
 
@@ -56,9 +63,15 @@ constexpr int WEPI0 = WNPW;  // first epilogue warp (a multiple of 4: warp % 4 i
 constexpr int WMMA = WEPI0 + WNEPI;
 constexpr int WTHREADS = (WMMA + 1) * 32;
 constexpr int WGS = 2;       // group metadata slots
-constexpr uint32_t A_OP = WG * WM * WKC;  // bf16 per stage of the home rows (hi or lo)
-constexpr uint32_t B_OP = WN * WKC;       // bf16 per stage of the candidate rows (hi or lo)
-constexpr uint32_t STAGE_ELEMS = 2 * A_OP + 2 * B_OP;
+// stage layout (bytes): home hi | home lo (64-byte rows, 64B swizzle, by TMA) |
+// candidates hi | candidates lo (no-swizzle core matrices, by cp.async)
+constexpr uint32_t A_CHUNK = WM * WKC * 2;      // one 128-row home chunk, hi or lo (8 KB)
+constexpr uint32_t A_LO = WG * A_CHUNK;         // 16 KB
+constexpr uint32_t B_HI = 2 * WG * A_CHUNK;     // 32 KB
+constexpr uint32_t B_LO = B_HI + WN * WKC * 2;  // 48 KB
+constexpr uint32_t STAGE_BYTES = B_LO + WN * WKC * 2;
+constexpr uint32_t SW_ATOM = 8 * WKC * 2;       // 8 rows x 64 B: the home rows' swizzle atom and MMA SBO
+constexpr uint32_t B_SBO = 16 * WKC;            // candidate rows, no swizzle: 8-row groups of WKC/8 core matrices
 constexpr uint32_t WFLAG_END = 1;
 static_assert(WNPROD == WG * WM && WNPROD == WN, "one producer thread per operand row");
 
@@ -86,25 +99,57 @@ struct WShared {
   uint32_t abort_flag;
   uint32_t tmem_base;
   uint32_t pflag[2];
-  unsigned long long full[WNS], sfree[WNS], dfull[WG], dfree[WG], gfree[WGS];
+  unsigned long long full[WNS], afull[WNS], sfree[WNS], dfull[WG], dfree[WG], gfree[WGS];
 };
 
 __device__ __forceinline__ void wprod_sync() { asm volatile("bar.sync 1, %0;" ::"n"(WNPROD) : "memory"); }
 
-__device__ __forceinline__ void cp_async16_ca(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+// The tensor maps over the split rows (hi, lo): home-row tiles of 128 rows x
+// 32 bf16, 64B swizzle.
+struct TcwMaps {
+  CUtensorMap ah, al;
+};
+
+// tcgen05 shared-memory descriptor, K-major, 64B swizzle: 64-byte rows,
+// 8-row atoms of 512 B (SBO); LBO is not used by swizzled K-major layouts.
+__device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)((SW_ATOM >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version
+  d |= (uint64_t)4 << 61;  // layout: 64B swizzle
+  return d;
+}
+
+__device__ __forceinline__ void cp_async16_s(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+// 2-D tile load (x: first element, a multiple of 8 bf16; y: first row).
+__device__ __forceinline__ void tma_tile_2d(uint32_t dst, uint64_t map, int x, int y, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(map), "r"(x), "r"(y), "r"(mbar)
+      : "memory");
 }
 
 // One warp per sorted row: bf16 hi/lo split of the FP32 row (zero beyond its
-// dpad32 stored values, up to kd) and its FP32 squared norm.  Output row layout: kd / 8 blocks of
-// [hi: 8 bf16 | lo: 8 bf16].
+// dpad32 stored values, up to kd) into the row-major arrays xh, xl (kd bf16
+// a row), and its FP32 squared norm.
 __global__ void k_split_rows(const float* __restrict__ xf, uint32_t dpad32, uint32_t kd, size_t n,
-                             uint4* __restrict__ xw, float* __restrict__ xn) {
+                             uint4* __restrict__ xh, uint4* __restrict__ xl, float* __restrict__ xn) {
   const size_t row = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
   const float* x = xf + row * dpad32;
-  uint4* out = xw + row * (kd / 8) * 2;
+  uint4* oh_row = xh + row * (kd / 8);
+  uint4* ol_row = xl + row * (kd / 8);
   float acc = 0.f;
   for (uint32_t kb = lane; kb < kd / 8; kb += 32) {
     float v[8];
@@ -128,8 +173,8 @@ __global__ void k_split_rows(const float* __restrict__ xf, uint32_t dpad32, uint
       ph[i] = *reinterpret_cast<const uint32_t*>(&hv);
       pl[i] = *reinterpret_cast<const uint32_t*>(&lv);
     }
-    out[2 * kb] = oh;
-    out[2 * kb + 1] = ol;
+    oh_row[kb] = oh;
+    ol_row[kb] = ol;
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(FULL_MASK, acc, o);
@@ -138,12 +183,11 @@ __global__ void k_split_rows(const float* __restrict__ xf, uint32_t dpad32, uint
 
 // ---------------------------------------------------------------- pipeline
 // One persistent CTA per SM: 8 producer warps, 8 epilogue warps, 1 MMA warp.
-//   producers  fetch units; per group of up to 256 candidates compute the
-//              columns' ids, norms and thresholds, then for each K chunk
-//              copy the chunk of the home rows (thread t: row t) and of the
-//              candidate rows (thread t: column t) into the next stage with
-//              cp.async; a stage is published (full) once its copies have
-//              landed, one stage behind the newest issued one;
+//   producers  fetch units; per group of up to 256 candidates all 8 warps
+//              compute the columns' sorted positions, ids, norms and
+//              thresholds; warp 0 then issues, per K chunk, the stage's TMA
+//              copies (home tiles + candidate gathers) against one
+//              expect_tx on the stage's full barrier;
 //   MMA warp   one lane issues 2 x 3 tcgen05.mma (K 16, M 128, N up to 256)
 //              per home chunk and stage, commits each stage to sfree and, at
 //              a group's last stage, each accumulator to dfull;
@@ -151,25 +195,28 @@ __global__ void k_split_rows(const float* __restrict__ xf, uint32_t dpad32, uint
 //              sign-bit test, home-bin rule by column range, sure accepts
 //              to the pair list, the error band to the band list.
 // Barriers (all waits bounded by a %globaltimer deadline):
-//   full[s]   producers -> MMA       (WNPROD arrivals)
+//   full[s]   producers -> MMA       (one arrive.expect_tx + the TMA bytes)
 //   sfree[s]  MMA -> producers       (tcgen05.commit: stage s read)
 //   dfull[g]  MMA -> epilogue        (tcgen05.commit, or a plain arrive to stop)
 //   dfree[g]  epilogue -> MMA        (WNEPI arrivals; accumulator g reusable)
 //   gfree[x]  epilogue -> producers  (WNEPI arrivals; group slot x reusable)
-__global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, const TcParams T) {
-  extern __shared__ __align__(128) unsigned char tcw_dyn[];
+__global__ void __launch_bounds__(WTHREADS, 1)
+    k_join_tcw(const JoinParams P, const TcParams T, const __grid_constant__ TcwMaps M) {
+  extern __shared__ __align__(1024) unsigned char tcw_dyn[];
   __shared__ WShared S;
-  __nv_bfloat16* stages = reinterpret_cast<__nv_bfloat16*>(tcw_dyn);  // WNS x [Ahi | Alo | Bhi | Blo]
-  unsigned long long* pstage = reinterpret_cast<unsigned long long*>(stages + WNS * STAGE_ELEMS);
+  // stages: WNS x STAGE_BYTES from the first 1024-byte boundary (swizzle atoms
+  // must sit on their natural alignment); then the pair staging buffers
+  const uint32_t dyn0 = smem_u32(tcw_dyn);
+  const uint32_t stage_base = (dyn0 + 1023u) & ~1023u;
+  unsigned long long* pstage = reinterpret_cast<unsigned long long*>(tcw_dyn + (stage_base - dyn0) + WNS * STAGE_BYTES);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint4* XW = T.xw;
-  const uint32_t kb_row = T.kd / 8;  // K blocks per row
   const uint32_t nkc = T.kd / WKC;   // stages per group
   volatile uint32_t* abort_flag = &S.abort_flag;
 
   if (tid == 0) {
     for (int i = 0; i < WNS; ++i) {
       mbar_init(&S.full[i], WNPROD);
+      mbar_init(&S.afull[i], 1);
       mbar_init(&S.sfree[i], 1);
     }
     for (int i = 0; i < WG; ++i) {
@@ -192,14 +239,19 @@ __global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, co
 
   if (warp < WNPW) {
     // ============================ producers
-    // Every branch that leads to bar.sync is taken on a value all producer
-    // threads hold in registers or read from shared memory after the same
-    // bar.sync; barrier waits are done by thread 0 and broadcast through
-    // S.pflag[2] (a thread is at most one bar.sync behind thread 0).
+    // All 8 warps prepare each group (candidate positions, ids, thresholds);
+    // warp 0 then issues the group's stages as TMA copies.  Every branch that
+    // leads to bar.sync is taken on a value all producer threads hold in
+    // registers or read from shared memory after the same bar.sync; barrier
+    // waits shared by all producers are done by thread 0 and broadcast
+    // through S.pflag[2] (a thread is at most one bar.sync behind thread 0).
     const uint32_t t = (uint32_t)tid;
-    uint32_t step = 0, pub = 0, group = 0, pf = 0, wgen = 0;
+    uint32_t step = 0, group = 0, pf = 0, wgen = 0;
     unsigned long long n_tiles = 0, n_cells = 0;
     bool aborted = false;
+    long long pc_grp = 0, pc_sfree = 0, pc_issue = 0, pc_pub = 0;  // cycles (T.prof)
+    const long long p_start = T.prof ? clock64() : 0;
+    const uint64_t map_ah = reinterpret_cast<uint64_t>(&M.ah), map_al = reinterpret_cast<uint64_t>(&M.al);
     // thread 0 waits on b (bounded), all producers learn the outcome
     auto shared_wait = [&](unsigned long long* b, uint32_t parity) -> bool {
       const uint32_t sl = pf++ & 1;
@@ -207,7 +259,9 @@ __global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, co
       wprod_sync();
       return S.pflag[sl] != 0u;
     };
-    // publishes every issued stage but the newest `keep` once its copies landed
+    // publishes every issued stage's candidate rows but the newest `keep`
+    // once this thread's copies have landed
+    uint32_t pub = 0;
     auto publish = [&](uint32_t keep) {
       while (pub + keep < step) {
         if (step - pub > 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
@@ -217,6 +271,10 @@ __global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, co
         ++pub;
       }
     };
+    const uint16_t* XH = static_cast<const uint16_t*>(T.xh);
+    const uint16_t* XL = static_cast<const uint16_t*>(T.xl);
+    const uint32_t prow0 = 32u * (uint32_t)warp + ((uint32_t)lane >> 2);  // + 8 i
+    const uint32_t pkb = ((uint32_t)lane >> 1) & 1u, ph = (uint32_t)lane & 1u;
     for (;;) {
       const uint32_t slot = pf++ & 1;
       if (tid == 0) {
@@ -243,7 +301,6 @@ __global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, co
       }
       wprod_sync();
       const float ra2max = __uint_as_float(S.ra2max);
-      const uint4* arow_src = XW + (size_t)(a0 + t) * kb_row * 2;
 
       uint32_t seg_next = U.s0, w_nb = 0, w_pos = 0, w_total = 0;
       int w_hj = -1;
@@ -279,11 +336,14 @@ __global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, co
           seg_next += nb;
         }
         // ---- a group: columns [w_pos, w_pos + ncols) of the window
+        const long long cg0 = T.prof ? clock64() : 0;
         const uint32_t ncols = min((uint32_t)WN, w_total - w_pos);
         const bool bcol = t < ncols;
+        // sorted position of column t (columns past ncols: the first one,
+        // never loaded)
         uint32_t q = 0;
-        if (bcol) {
-          const uint32_t rank = w_pos + t;
+        {
+          const uint32_t rank = w_pos + (bcol ? t : 0u);
           int lo = 0, hi = (int)w_nb - 1;
           while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
@@ -337,31 +397,58 @@ __global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, co
           n_tiles += (unsigned long long)ng * ((ncols + 127) / 128);
           n_cells += (unsigned long long)nrows * ncols;
         }
-        const uint4* bsrc = XW + (size_t)q * kb_row * 2;
+        if (T.prof) pc_grp += clock64() - cg0;
+        // ---- the group's K chunks, one stage each: the home rows as 128-row
+        // TMA tiles (thread 0, against one expect_tx on afull), the candidate
+        // rows by cp.async, lane l of warp w moving rows 32w + 8i + l / 4
+        // (i = 0..3), piece l % 4 (K block 2j + (l % 4) / 2 of pair j, hi or
+        // lo by l % 2): 8 rows x 64 contiguous bytes per instruction, 16-byte
+        // chunks without shared-memory bank conflicts
+        const uint16_t* b_src[4];
+        uint32_t b_ok = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const uint32_t qi = __shfl_sync(FULL_MASK, q, 8 * i + (lane >> 2));  // column prow0 + 8 i
+          b_src[i] = (ph ? XL : XH) + (size_t)qi * T.kd;
+          if (prow0 + 8 * i < ncols) b_ok |= 1u << i;
+        }
+        const uint32_t abytes = ng * 2u * A_CHUNK;
         for (uint32_t kc = 0; kc < nkc; ++kc) {
           const uint32_t s = step % WNS;
+          const long long cs0 = T.prof ? clock64() : 0;
           if (!shared_wait(&S.sfree[s], ((step / WNS) & 1) ^ 1)) {
             aborted = true;
             break;
           }
-          __nv_bfloat16* st = stages + s * STAGE_ELEMS;
-          __nv_bfloat16 *ahi = st, *alo = st + A_OP, *bhi = st + 2 * A_OP, *blo = bhi + B_OP;
-#pragma unroll
-          for (int j = 0; j < WKC / 8; ++j) {
-            const uint32_t gkb = kc * (WKC / 8) + j;  // K block within the row
-            const uint32_t off = chunk_off<WKC>(t, j);
-            if (arow) {
-              cp_async16_ca(ahi + off, arow_src + 2 * gkb);
-              cp_async16_ca(alo + off, arow_src + 2 * gkb + 1);
+          const long long cs1 = T.prof ? clock64() : 0;
+          const uint32_t sb = stage_base + s * STAGE_BYTES;
+          if (tid == 0) {
+            const uint32_t ab = smem_u32(&S.afull[s]);
+            mbar_expect_tx(ab, abytes);
+            for (uint32_t g = 0; g < ng; ++g) {
+              tma_tile_2d(sb + g * A_CHUNK, map_ah, (int)(kc * WKC), (int)(a0 + g * WM), ab);
+              tma_tile_2d(sb + A_LO + g * A_CHUNK, map_al, (int)(kc * WKC), (int)(a0 + g * WM), ab);
             }
-            if (bcol) {
-              cp_async16_ca(bhi + off, bsrc + 2 * gkb);
-              cp_async16_ca(blo + off, bsrc + 2 * gkb + 1);
+          }
+          const uint32_t bdst = sb + (ph ? B_LO : B_HI);
+#pragma unroll
+          for (int j = 0; j < WKC / 16; ++j) {
+            const uint32_t kb = 2 * j + pkb;  // K block within the stage
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const uint32_t off = 2u * chunk_off<WKC>(prow0 + 8 * i, kb);
+              if (b_ok & (1u << i)) cp_async16_s(bdst + off, b_src[i] + kc * WKC + kb * 8);
             }
           }
           asm volatile("cp.async.commit_group;" ::: "memory");
           ++step;
+          const long long cs2 = T.prof ? clock64() : 0;
           publish(1);
+          if (T.prof) {
+            pc_sfree += cs1 - cs0;
+            pc_issue += cs2 - cs1;
+            pc_pub += clock64() - cs2;
+          }
         }
         if (aborted) break;
         w_pos += ncols;
@@ -379,25 +466,44 @@ __global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, co
         if (tid == 0) S.grp[gs].flags = WFLAG_END;
         wprod_sync();
         mbar_arrive(&S.full[s]);
+        if (tid == 0) mbar_arrive(&S.afull[s]);
       }
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
+    // an aborting CTA may still have TMA copies in flight into its stages:
+    // wait (bounded) until each stage's last issued home tiles have landed
+    if (tid == 0 && *abort_flag) {
+      volatile uint32_t no_abort = 0;
+      for (uint32_t j = step > WNS ? step - WNS : 0; j < step; ++j)
+        wait_or_abort(&S.afull[j % WNS], (j / WNS) & 1, &no_abort, T.wait_limit);
+    }
     if (tid == 0 && n_tiles) {
       atomicAdd(&T.ctr->tiles, n_tiles);
       atomicAdd(&T.ctr->cells, n_cells);
     }
+    if (tid == 0 && T.prof) {
+      atomicAdd(&T.ctr->prof[1], (unsigned long long)(clock64() - p_start));
+      atomicAdd(&T.ctr->prof[7], (unsigned long long)pc_grp);
+      atomicAdd(&T.ctr->prof[0], (unsigned long long)pc_sfree);
+      atomicAdd(&T.ctr->prof[9], (unsigned long long)pc_issue);
+      atomicAdd(&T.ctr->prof[14], (unsigned long long)pc_pub);
+    }
   } else if (warp == WMMA) {
     // ============================ MMA issuer
     if (lane == 0) {
-      constexpr uint32_t SBO = 16u * WKC;
       uint32_t step = 0, group = 0;
       uint32_t use[WG] = {0, 0};
       unsigned long long* last_bar = nullptr;
       uint32_t last_par = 0;
       bool ok = true;
+      long long mw_full = 0, mw_dfree = 0;
+      const long long m_start = T.prof ? clock64() : 0;
       while (ok) {
         uint32_t s = step % WNS;
-        ok = wait_or_abort(&S.full[s], (step / WNS) & 1, abort_flag, T.wait_limit);
+        const long long c0 = T.prof ? clock64() : 0;
+        ok = wait_or_abort(&S.full[s], (step / WNS) & 1, abort_flag, T.wait_limit) &&
+             wait_or_abort(&S.afull[s], (step / WNS) & 1, abort_flag, T.wait_limit);
+        if (T.prof) mw_full += clock64() - c0;
         if (!ok) break;
         const WGroup& Gm = S.grp[group % WGS];
         if (Gm.flags & WFLAG_END) {
@@ -410,26 +516,35 @@ __global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, co
         for (uint32_t kc = 0; kc < nkc && ok; ++kc) {
           if (kc > 0) {
             s = step % WNS;
-            ok = wait_or_abort(&S.full[s], (step / WNS) & 1, abort_flag, T.wait_limit);
+            const long long c1 = T.prof ? clock64() : 0;
+            ok = wait_or_abort(&S.full[s], (step / WNS) & 1, abort_flag, T.wait_limit) &&
+                 wait_or_abort(&S.afull[s], (step / WNS) & 1, abort_flag, T.wait_limit);
+            if (T.prof) mw_full += clock64() - c1;
             if (!ok) break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
-          const __nv_bfloat16* st = stages + s * STAGE_ELEMS;
-          const uint32_t bh = smem_u32(st + 2 * A_OP), bl = smem_u32(st + 2 * A_OP + B_OP);
+          const uint32_t sb = stage_base + s * STAGE_BYTES;
+          const uint32_t bh = sb + B_HI, bl = sb + B_LO;
           for (uint32_t g = 0; g < ng; ++g) {
             if (kc == 0) {  // first writes of this group into accumulator g
+              const long long c2 = T.prof ? clock64() : 0;
               ok = wait_or_abort(&S.dfree[g], (use[g] & 1) ^ 1, abort_flag, T.wait_limit);
+              if (T.prof) mw_dfree += clock64() - c2;
               if (!ok) break;
               asm volatile("tcgen05.fence::after_thread_sync;");
             }
-            const uint32_t ah = smem_u32(st + g * WM * WKC), al = smem_u32(st + A_OP + g * WM * WKC);
+            const uint32_t ah = sb + g * A_CHUNK, al = sb + A_LO + g * A_CHUNK;
             const uint32_t dt = tbase + g * WN;
 #pragma unroll
             for (int ks = 0; ks < WKC / 16; ++ks) {
-              const uint32_t o = ks * 256;  // two K blocks of 128 B
-              mma_bf16(dt, umma_desc(ah + o, SBO), umma_desc(bh + o, SBO), idesc, (kc | ks) ? 1u : 0u);
-              mma_bf16(dt, umma_desc(ah + o, SBO), umma_desc(bl + o, SBO), idesc, 1u);
-              mma_bf16(dt, umma_desc(al + o, SBO), umma_desc(bh + o, SBO), idesc, 1u);
+              // K step of 16 bf16: 32 bytes into the home rows' 64-byte swizzled
+              // rows, two 128-byte core-matrix columns into the candidate rows
+              const uint32_t oa = ks * 32, ob = ks * 256;
+              const uint64_t dah = desc_sw64(ah + oa), dal = desc_sw64(al + oa);
+              const uint64_t dbh = umma_desc(bh + ob, B_SBO), dbl = umma_desc(bl + ob, B_SBO);
+              mma_bf16(dt, dah, dbh, idesc, (kc | ks) ? 1u : 0u);
+              mma_bf16(dt, dah, dbl, idesc, 1u);
+              mma_bf16(dt, dal, dbh, idesc, 1u);
             }
           }
           if (!ok) break;
@@ -446,6 +561,12 @@ __global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, co
           ++use[g];
         }
         ++group;
+      }
+      if (T.prof) {
+        atomicAdd(&T.ctr->prof[2], (unsigned long long)mw_full);
+        atomicAdd(&T.ctr->prof[3], (unsigned long long)mw_dfree);
+        atomicAdd(&T.ctr->prof[4], (unsigned long long)(clock64() - m_start));
+        atomicAdd(&T.ctr->prof[12], (unsigned long long)step);
       }
       // an aborting CTA may still have MMAs in flight: wait (bounded) for the
       // last commit, MMAs complete in issue order
@@ -466,13 +587,17 @@ __global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, co
     uint32_t group = 0;
     uint32_t use[WG] = {0, 0};
     bool run = true;
+    long long ew = 0;
+    const long long e_start = T.prof ? clock64() : 0;
     while (run) {
       const uint32_t gs = group % WGS;
       const WGroup& Gm = S.grp[gs];
       uint32_t ng = 1;
       for (uint32_t g = 0; g < ng; ++g) {
         // all lanes wait; the outcome is made warp-uniform (tcgen05.ld is .sync.aligned)
+        const long long cw = T.prof ? clock64() : 0;
         const bool ok = __all_sync(FULL_MASK, wait_or_abort(&S.dfull[g], use[g] & 1, abort_flag, T.wait_limit));
+        if (T.prof) ew += clock64() - cw;
         if (!ok || __any_sync(FULL_MASK, (Gm.flags & WFLAG_END) || *abort_flag)) {
           run = false;
           break;
@@ -556,6 +681,10 @@ __global__ void __launch_bounds__(WTHREADS, 1) k_join_tcw(const JoinParams P, co
     }
     stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
     stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap);
+    if (T.prof && lane == 0) {
+      atomicAdd(&T.ctr->prof[5], (unsigned long long)ew);
+      atomicAdd(&T.ctr->prof[6], (unsigned long long)(clock64() - e_start));
+    }
   }
   // all roles meet here before tensor memory is released
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -570,19 +699,51 @@ namespace join {
 
 uint32_t tcw_kd(uint32_t d) { return (d + WKC - 1) / WKC * WKC; }
 
-void tcw_prepare(mistic_handle_s* h, const float* xf, uint32_t dpad32, uint32_t d, size_t n, uint4* xw, float* xn) {
+void tcw_prepare(mistic_handle_s* h, const float* xf, uint32_t dpad32, uint32_t d, size_t n, void* xh, void* xl,
+                 float* xn) {
   if (n == 0) return;
   const unsigned rows_per_block = 8;
   const unsigned grid = (unsigned)((n + rows_per_block - 1) / rows_per_block);
-  k_split_rows<<<grid, rows_per_block * 32, 0, h->stream>>>(xf, dpad32, tcw_kd(d), n, xw, xn);
+  k_split_rows<<<grid, rows_per_block * 32, 0, h->stream>>>(xf, dpad32, tcw_kd(d), n, (uint4*)xh, (uint4*)xl, xn);
   launched(h, "split_rows");
 }
 
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  });
+  if (!fn) throw Error(MISTIC_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  return fn;
+}
+
+// bf16 rows of kd elements (row pitch kd * 2 bytes), n rows; box: 32 x rows.
+void encode_rows(CUtensorMap* m, const void* base, uint32_t kd, size_t n, uint32_t box_rows) {
+  const cuuint64_t dims[2] = {kd, (cuuint64_t)n};
+  const cuuint64_t strides[1] = {(cuuint64_t)kd * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)WKC, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+                                 estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error(MISTIC_ERR_CUDA, "cuTensorMapEncodeTiled failed for the split rows");
+}
+}  // namespace
+
 void run_tcw(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
   if (T.n_units == 0) return;
-  if (!T.xw || !T.xn || T.kd % WKC) throw Error(MISTIC_ERR_INTERNAL, "long-row tensor-core join without split rows");
-  const size_t dyn = (size_t)WNS * STAGE_ELEMS * sizeof(__nv_bfloat16) +
-                     (size_t)2 * WNEPI * PSTAGE * sizeof(unsigned long long);
+  if (!T.xh || !T.xl || !T.xn || T.kd % WKC || T.n_rows == 0)
+    throw Error(MISTIC_ERR_INTERNAL, "long-row tensor-core join without split rows");
+  TcwMaps maps;
+  encode_rows(&maps.ah, T.xh, T.kd, T.n_rows, WM);
+  encode_rows(&maps.al, T.xl, T.kd, T.n_rows, WM);
+  const size_t dyn = 1024 + (size_t)WNS * STAGE_BYTES + (size_t)2 * WNEPI * PSTAGE * sizeof(unsigned long long);
   MCK(cudaFuncSetAttribute(k_join_tcw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
   MCK(cudaFuncSetAttribute(k_join_tcw, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
@@ -592,7 +753,7 @@ void run_tcw(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
   if (getenv("MISTIC_DEBUG"))
     fprintf(stderr, "[mistic] join_tcw KD=%u dyn=%zu occupancy=%d grid=%u units=%llu\n", T.kd, dyn, per_sm, grid,
             (unsigned long long)T.n_units);
-  k_join_tcw<<<grid, WTHREADS, dyn, h->stream>>>(P, T);
+  k_join_tcw<<<grid, WTHREADS, dyn, h->stream>>>(P, T, maps);
   launched(h, "join_tcw");
 }
 

@@ -588,11 +588,14 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     tp.prof = getenv("MISTIC_DEBUG") ? 1 : 0;
     if (wide && tots[2] > 0) {
       tp.kd = join::tcw_kd(d);
-      uint4* xw = abuf<uint4>(h, "xw", n * (size_t)(tp.kd / 8) * 2);
+      uint16_t* xh = abuf<uint16_t>(h, "xh", n * (size_t)tp.kd);
+      uint16_t* xl = abuf<uint16_t>(h, "xl", n * (size_t)tp.kd);
       float* xn = abuf<float>(h, "xn", n);
-      join::tcw_prepare(h, xf, dpad32, d, n, xw, xn);
-      tp.xw = xw;
+      join::tcw_prepare(h, xf, dpad32, d, n, xh, xl, xn);
+      tp.xh = xh;
+      tp.xl = xl;
       tp.xn = xn;
+      tp.n_rows = n;
     }
   }
   const bool want_pairs = o.pairs != MISTIC_PAIRS_NONE;
@@ -617,7 +620,10 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   jp.ctr = ctr;
   // band list: pairs the FP32 / tensor-core joins leave to the FP64 check
   if (!fp64) {
+    // measured band fractions are ~2e-5 - 5e-5 of the candidate pairs; start
+    // above that so the first call rarely has to run the join again
     unsigned long long bcap = std::max<unsigned long long>(1ull << 20, 2ull * n);
+    bcap = std::max<unsigned long long>(bcap, std::min<unsigned long long>(totc / 8192, 1ull << 30));
     auto it = h->arena.bufs.find("band");
     if (it != h->arena.bufs.end()) bcap = std::max<unsigned long long>(bcap, it->second.bytes / 8);
     // MISTIC_BAND_CAP=k starts from a k-entry list (tests of the overflow path)
@@ -657,7 +663,16 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     d2h(h, &tcc, ctr + 1, sizeof tcc);
     r->tc_tiles = tcc.tiles;
     r->tc_cells = tcc.cells;
-    if (tp.prof) {
+    if (tp.prof && tp.xh) {
+      const double tot_p = (double)tcc.prof[1], tot_m = (double)tcc.prof[4], tot_e = (double)tcc.prof[6];
+      fprintf(stderr,
+              "[mistic] join_tcw roles: producers group setup %.1f%% stage wait %.1f%% issue %.1f%% publish %.1f%% | "
+              "MMA wait-full %.1f%% wait-acc %.1f%% | epilogue wait %.1f%% | %llu stages\n",
+              tot_p ? 100.0 * tcc.prof[7] / tot_p : 0.0, tot_p ? 100.0 * tcc.prof[0] / tot_p : 0.0,
+              tot_p ? 100.0 * tcc.prof[9] / tot_p : 0.0, tot_p ? 100.0 * tcc.prof[14] / tot_p : 0.0,
+              tot_m ? 100.0 * tcc.prof[2] / tot_m : 0.0, tot_m ? 100.0 * tcc.prof[3] / tot_m : 0.0,
+              tot_e ? 100.0 * tcc.prof[5] / tot_e : 0.0, (unsigned long long)tcc.prof[12]);
+    } else if (tp.prof) {
       const double tot_p = (double)tcc.prof[1], tot_m = (double)tcc.prof[4], tot_e = (double)tcc.prof[6];
       fprintf(stderr,
               "[mistic] join_tc roles: producers wait-for-free-stage %.1f%% | MMA wait-full %.1f%% wait-free-acc "
