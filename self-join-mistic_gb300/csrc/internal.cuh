@@ -167,6 +167,10 @@ struct mistic_handle_s {
   mistic::Arena arena;
   void* pinned = nullptr;  // small pinned block for scalar read-backs
   size_t pinned_bytes = 0;
+  // pinned staging ring for large host inputs (mistic::h2d): kStageSlots
+  // slots of kStageSlotBytes, each with the event of its last DMA
+  void* stage = nullptr;
+  cudaEvent_t stage_ev[16] = {};
   cudaEvent_t ev[16] = {};
   cudaEvent_t jev[4] = {};  // around the two join kernels
   uint32_t launches = 0;

@@ -218,8 +218,72 @@ void d2h(mistic_handle_s* h, void* dst, const void* src, size_t bytes) {
   MCK(cudaStreamSynchronize(h->stream));
 }
 
+// Host -> device copy of a caller's (pageable) array, stream-ordered on the
+// handle's stream.  Small copies go straight to cudaMemcpyAsync.  Large ones
+// go through the handle's pinned staging ring: kStageThreads host threads
+// each copy every kStageThreads-th chunk into one of their two slots and
+// issue that slot's DMA, so the host-side copies run in parallel and overlap
+// the DMAs (a pageable cudaMemcpyAsync is one driver-staged copy at a time,
+// measured at 7.3 GB/s for the 720 MB input of the 5M x 18 join).  The
+// ring (128 MB pinned) is allocated at the handle's first large copy.  A slot is
+// refilled only after the event recorded behind its previous DMA has
+// completed.  The call returns once every DMA has been issued; the source
+// may be reused by the caller after the stream has passed them.
+constexpr size_t kStageSlotBytes = 8u << 20;
+constexpr int kStageThreads = 8;
+constexpr int kStageSlots = 2 * kStageThreads;
+constexpr size_t kStageMin = 128u << 20;
+static_assert(kStageSlots <= (int)(sizeof(((mistic_handle_s*)nullptr)->stage_ev) / sizeof(cudaEvent_t)),
+              "one event per staging slot");
+
 void h2d(mistic_handle_s* h, void* dst, const void* src, size_t bytes) {
-  MCK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
+  if (bytes >= kStageMin && !h->stage) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, kStageSlots * kStageSlotBytes, cudaHostAllocPortable) == cudaSuccess) {
+      bool ok = true;
+      for (int i = 0; i < kStageSlots && ok; ++i)
+        ok = cudaEventCreateWithFlags(&h->stage_ev[i], cudaEventDisableTiming) == cudaSuccess;
+      if (ok) {
+        h->stage = p;
+      } else {
+        for (auto& e : h->stage_ev)
+          if (e) cudaEventDestroy(e), e = nullptr;
+        cudaFreeHost(p);
+      }
+    }
+    cudaGetLastError();  // no staging ring: the plain copy below
+  }
+  if (bytes < kStageMin || !h->stage) {
+    MCK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    return;
+  }
+  const size_t nchunks = (bytes + kStageSlotBytes - 1) / kStageSlotBytes;
+  std::atomic<int> err{(int)cudaSuccess};
+  auto worker = [&](int t) {
+    cudaSetDevice(h->device);
+    uint32_t use = 0;
+    for (size_t c = (size_t)t; c < nchunks && err.load() == (int)cudaSuccess; c += kStageThreads, ++use) {
+      const int slot = t + kStageThreads * (int)(use & 1);
+      unsigned char* sb = static_cast<unsigned char*>(h->stage) + (size_t)slot * kStageSlotBytes;
+      const size_t off = c * kStageSlotBytes, len = std::min(kStageSlotBytes, bytes - off);
+      cudaError_t e = cudaEventSynchronize(h->stage_ev[slot]);  // the slot's previous DMA is done
+      if (e == cudaSuccess) {
+        memcpy(sb, static_cast<const unsigned char*>(src) + off, len);
+        e = cudaMemcpyAsync(static_cast<unsigned char*>(dst) + off, sb, len, cudaMemcpyHostToDevice, h->stream);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(h->stage_ev[slot], h->stream);
+      if (e != cudaSuccess) {
+        int ok = (int)cudaSuccess;
+        err.compare_exchange_strong(ok, (int)e);
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  const int nt = (int)std::min<size_t>(kStageThreads, nchunks);
+  for (int t = 1; t < nt; ++t) pool.emplace_back(worker, t);
+  worker(0);
+  for (auto& th : pool) th.join();
+  MCK((cudaError_t)err.load());
 }
 
 struct PhaseClock {
@@ -921,6 +985,9 @@ mistic_status mistic_destroy(mistic_handle h) {
   cudaStreamSynchronize(h->stream);
   h->arena.release_all();
   if (h->pinned) cudaFreeHost(h->pinned);
+  if (h->stage) cudaFreeHost(h->stage);
+  for (auto& e : h->stage_ev)
+    if (e) cudaEventDestroy(e);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : h->jev)
