@@ -15,9 +15,10 @@
 // join: operands stream from L2 into shared memory in K chunks of 32.  The
 // home rows (contiguous) come as 128-row TMA tiles (cp.async.bulk.tensor,
 // 64-byte rows, 64B swizzle); the candidate rows, which come from several
-// bins, by cp.async in 16-byte chunks into no-swizzle core matrices.  (TMA
+// bins, by cp.async in 16-byte chunks written to the same swizzled layout
+// (the MMAs ran 25% faster on it than on no-swizzle core matrices).  TMA
 // 4-row gathers of the candidate rows were measured slower: 64-byte rows
-// keep the copy engine busy far longer than the MMAs take.)
+// keep the copy engine busy far longer than the MMAs take.
 //
 // Tiles: 2 home chunks of 128 rows (MMA M = 128 each) x up to 256 candidate
 // columns (MMA N), i.e. two 128 x 256 FP32 accumulators = all 512 TMEM
@@ -63,15 +64,14 @@ constexpr int WEPI0 = WNPW;  // first epilogue warp (a multiple of 4: warp % 4 i
 constexpr int WMMA = WEPI0 + WNEPI;
 constexpr int WTHREADS = (WMMA + 1) * 32;
 constexpr int WGS = 2;       // group metadata slots
-// stage layout (bytes): home hi | home lo (64-byte rows, 64B swizzle, by TMA) |
-// candidates hi | candidates lo (no-swizzle core matrices, by cp.async)
+// stage layout (bytes): home hi | home lo (by TMA) | candidates hi |
+// candidates lo (by cp.async), all as 64-byte rows in the 64B swizzle
 constexpr uint32_t A_CHUNK = WM * WKC * 2;      // one 128-row home chunk, hi or lo (8 KB)
 constexpr uint32_t A_LO = WG * A_CHUNK;         // 16 KB
 constexpr uint32_t B_HI = 2 * WG * A_CHUNK;     // 32 KB
 constexpr uint32_t B_LO = B_HI + WN * WKC * 2;  // 48 KB
 constexpr uint32_t STAGE_BYTES = B_LO + WN * WKC * 2;
 constexpr uint32_t SW_ATOM = 8 * WKC * 2;       // 8 rows x 64 B: the home rows' swizzle atom and MMA SBO
-constexpr uint32_t B_SBO = 16 * WKC;            // candidate rows, no swizzle: 8-row groups of WKC/8 core matrices
 constexpr uint32_t WFLAG_END = 1;
 static_assert(WNPROD == WG * WM && WNPROD == WN, "one producer thread per operand row");
 
@@ -99,7 +99,7 @@ struct WShared {
   uint32_t abort_flag;
   uint32_t tmem_base;
   uint32_t pflag[2];
-  unsigned long long full[WNS], afull[WNS], sfree[WNS], dfull[WG], dfree[WG], gfree[WGS];
+  unsigned long long full[WNS], afull[WNS], sfree[WNS], dfull[WG], dfree[WG], gfree[WGS], gready[WGS];
 };
 
 __device__ __forceinline__ void wprod_sync() { asm volatile("bar.sync 1, %0;" ::"n"(WNPROD) : "memory"); }
@@ -124,6 +124,13 @@ __device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
 
 __device__ __forceinline__ void cp_async16_s(uint32_t dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+// Arrive on `bar` once every cp.async this thread issued before has
+// completed (the barrier's expected count is not raised: the arrival counts
+// as one of its initial ones).
+__device__ __forceinline__ void cp_async_arrive_noinc(unsigned long long* bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
@@ -195,7 +202,9 @@ __global__ void k_split_rows(const float* __restrict__ xf, uint32_t dpad32, uint
 //              sign-bit test, home-bin rule by column range, sure accepts
 //              to the pair list, the error band to the band list.
 // Barriers (all waits bounded by a %globaltimer deadline):
-//   full[s]   producers -> MMA       (one arrive.expect_tx + the TMA bytes)
+//   full[s]   producers -> MMA       (WNPROD cp.async arrivals: candidate rows landed)
+//   afull[s]  producer 0 -> MMA      (one arrive.expect_tx + the TMA bytes of the home tiles)
+//   gready[x] producers -> MMA       (WNPROD arrivals: group slot x written)
 //   sfree[s]  MMA -> producers       (tcgen05.commit: stage s read)
 //   dfull[g]  MMA -> epilogue        (tcgen05.commit, or a plain arrive to stop)
 //   dfree[g]  epilogue -> MMA        (WNEPI arrivals; accumulator g reusable)
@@ -223,7 +232,10 @@ __global__ void __launch_bounds__(WTHREADS, 1)
       mbar_init(&S.dfull[i], 1);
       mbar_init(&S.dfree[i], WNEPI);
     }
-    for (int i = 0; i < WGS; ++i) mbar_init(&S.gfree[i], WNEPI);
+    for (int i = 0; i < WGS; ++i) {
+      mbar_init(&S.gfree[i], WNEPI);
+      mbar_init(&S.gready[i], WNPROD);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;");
     S.abort_flag = 0;
     S.w_home = 0xffffffffu;
@@ -258,18 +270,6 @@ __global__ void __launch_bounds__(WTHREADS, 1)
       if (tid == 0) S.pflag[sl] = wait_or_abort(b, parity, abort_flag, T.wait_limit) ? 1u : 0u;
       wprod_sync();
       return S.pflag[sl] != 0u;
-    };
-    // publishes every issued stage's candidate rows but the newest `keep`
-    // once this thread's copies have landed
-    uint32_t pub = 0;
-    auto publish = [&](uint32_t keep) {
-      while (pub + keep < step) {
-        if (step - pub > 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
-        else asm volatile("cp.async.wait_group 0;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_arrive(&S.full[pub % WNS]);
-        ++pub;
-      }
     };
     const uint16_t* XH = static_cast<const uint16_t*>(T.xh);
     const uint16_t* XL = static_cast<const uint16_t*>(T.xl);
@@ -397,13 +397,13 @@ __global__ void __launch_bounds__(WTHREADS, 1)
           n_tiles += (unsigned long long)ng * ((ncols + 127) / 128);
           n_cells += (unsigned long long)nrows * ncols;
         }
+        mbar_arrive(&S.gready[gs]);  // releases this thread's writes of the group slot
         if (T.prof) pc_grp += clock64() - cg0;
         // ---- the group's K chunks, one stage each: the home rows as 128-row
         // TMA tiles (thread 0, against one expect_tx on afull), the candidate
         // rows by cp.async, lane l of warp w moving rows 32w + 8i + l / 4
         // (i = 0..3), piece l % 4 (K block 2j + (l % 4) / 2 of pair j, hi or
-        // lo by l % 2): 8 rows x 64 contiguous bytes per instruction, 16-byte
-        // chunks without shared-memory bank conflicts
+        // lo by l % 2): 8 rows x 32 bytes of hi and of lo per instruction
         const uint16_t* b_src[4];
         uint32_t b_ok = 0;
 #pragma unroll
@@ -436,14 +436,17 @@ __global__ void __launch_bounds__(WTHREADS, 1)
             const uint32_t kb = 2 * j + pkb;  // K block within the stage
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-              const uint32_t off = 2u * chunk_off<WKC>(prow0 + 8 * i, kb);
+              const uint32_t r = prow0 + 8 * i;  // 64-byte row r, 16-byte chunk kb, 64B swizzle
+              const uint32_t off = r * 64u + ((kb ^ ((r >> 1) & 3u)) << 4);
               if (b_ok & (1u << i)) cp_async16_s(bdst + off, b_src[i] + kc * WKC + kb * 8);
             }
           }
-          asm volatile("cp.async.commit_group;" ::: "memory");
+          // this thread's arrival on the stage's full barrier is made by the
+          // copy engine once its copies above have landed: producers never
+          // block on their own copies, so all WNS stages can be in flight
+          cp_async_arrive_noinc(&S.full[s]);
           ++step;
           const long long cs2 = T.prof ? clock64() : 0;
-          publish(1);
           if (T.prof) {
             pc_sfree += cs1 - cs0;
             pc_issue += cs2 - cs1;
@@ -457,14 +460,13 @@ __global__ void __launch_bounds__(WTHREADS, 1)
       if (aborted) break;
     }
     if (!aborted) {
-      publish(0);
       // stop marker: a group slot flagged END behind a stage with no copies
       const uint32_t gs = group % WGS, s = step % WNS;
       bool ok = shared_wait(&S.gfree[gs], ((group / WGS) & 1) ^ 1);
       if (ok) ok = shared_wait(&S.sfree[s], ((step / WNS) & 1) ^ 1);
       if (ok) {
         if (tid == 0) S.grp[gs].flags = WFLAG_END;
-        wprod_sync();
+        mbar_arrive(&S.gready[gs]);
         mbar_arrive(&S.full[s]);
         if (tid == 0) mbar_arrive(&S.afull[s]);
       }
@@ -504,6 +506,8 @@ __global__ void __launch_bounds__(WTHREADS, 1)
         ok = wait_or_abort(&S.full[s], (step / WNS) & 1, abort_flag, T.wait_limit) &&
              wait_or_abort(&S.afull[s], (step / WNS) & 1, abort_flag, T.wait_limit);
         if (T.prof) mw_full += clock64() - c0;
+        // the group slot's metadata (written before the group's first stage)
+        if (ok) ok = wait_or_abort(&S.gready[group % WGS], (group / WGS) & 1, abort_flag, T.wait_limit);
         if (!ok) break;
         const WGroup& Gm = S.grp[group % WGS];
         if (Gm.flags & WFLAG_END) {
@@ -523,6 +527,10 @@ __global__ void __launch_bounds__(WTHREADS, 1)
             if (!ok) break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
+          // the candidate rows were written by cp.async (generic proxy) and
+          // are read by the MMAs (async proxy): this thread has acquired them
+          // through the full barrier; order them before its MMAs
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           const uint32_t sb = stage_base + s * STAGE_BYTES;
           const uint32_t bh = sb + B_HI, bl = sb + B_LO;
           for (uint32_t g = 0; g < ng; ++g) {
@@ -537,11 +545,11 @@ __global__ void __launch_bounds__(WTHREADS, 1)
             const uint32_t dt = tbase + g * WN;
 #pragma unroll
             for (int ks = 0; ks < WKC / 16; ++ks) {
-              // K step of 16 bf16: 32 bytes into the home rows' 64-byte swizzled
-              // rows, two 128-byte core-matrix columns into the candidate rows
-              const uint32_t oa = ks * 32, ob = ks * 256;
-              const uint64_t dah = desc_sw64(ah + oa), dal = desc_sw64(al + oa);
-              const uint64_t dbh = umma_desc(bh + ob, B_SBO), dbl = umma_desc(bl + ob, B_SBO);
+              // K step of 16 bf16: 32 bytes into the 64-byte swizzled rows of
+              // both operands
+              const uint32_t ok16 = ks * 32;
+              const uint64_t dah = desc_sw64(ah + ok16), dal = desc_sw64(al + ok16);
+              const uint64_t dbh = desc_sw64(bh + ok16), dbl = desc_sw64(bl + ok16);
               mma_bf16(dt, dah, dbh, idesc, (kc | ks) ? 1u : 0u);
               mma_bf16(dt, dah, dbl, idesc, 1u);
               mma_bf16(dt, dal, dbh, idesc, 1u);
