@@ -86,6 +86,9 @@ FALLBACK_PEAKS = {"hbm_gbs": 6785.9, "bf16_tflops": 1922.1, "bf16_tflops_sustain
 #: data, from the ncu capture of the 2.5M-point case (profiles/join_tc_susy18.md:
 #: 283.8 MB over 2.1993e10 cells); scaled by the cells of the measured launch.
 TC_DRAM_BYTES_PER_CELL_SUSY18 = 283.8e6 / 2.1993e10
+#: the same for k_join_tcw on the TINY-shaped data, from the capture of the
+#: 300k-point case (profiles/join_tcw_tiny384.md: 20.507 GB over 1.4457e10 cells)
+TCW_DRAM_BYTES_PER_CELL_TINY384 = 20.507e9 / 1.4457096836e10
 
 
 def load_peaks() -> dict:
@@ -386,6 +389,10 @@ def run_mistic(args, wl) -> None:
             roof["traffic"] = TC_DRAM_BYTES_PER_CELL_SUSY18 * r.tc_cells
             roof["traffic_source"] = ("ncu dram__bytes_read+write per cell of the 2.5M-point capture "
                                       "(profiles/join_tc_susy18.md) x this launch's cells")
+        elif args.workload == "tiny384" and wide:
+            roof["traffic"] = TCW_DRAM_BYTES_PER_CELL_TINY384 * r.tc_cells
+            roof["traffic_source"] = ("ncu dram__bytes_read+write per cell of the 300k-point capture "
+                                      "(profiles/join_tcw_tiny384.md) x this launch's cells")
     else:
         # dominant kernel: the FP32 filter join; 3*d flops per candidate pair
         # (d subtractions, d multiply-adds) on the CUDA-core FP32 pipe
