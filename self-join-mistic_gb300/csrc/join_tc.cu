@@ -590,7 +590,13 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         const uint32_t flags = S.meta[st].flags;
         const uint32_t ng = S.meta[st].ng;
         if (flags & FLAG_END) {
-          mbar_arrive(&S.dfull[mt % NACC]);
+          // wake the epilogue on the next accumulator, but only once every
+          // epilogue warp has taken that accumulator's previous use: an
+          // arrival before that would complete a second phase of dfull[b]
+          // under a warp still waiting for the first (parity aliasing)
+          const uint32_t b = mt % NACC;
+          wait_or_abort(&S.dfree[b], ((mt / NACC) & 1) ^ 1, abort_flag, T.wait_limit);
+          mbar_arrive(&S.dfull[b]);
           break;
         }
         bool ok = true;

@@ -511,6 +511,11 @@ __global__ void __launch_bounds__(WTHREADS, 1)
         if (!ok) break;
         const WGroup& Gm = S.grp[group % WGS];
         if (Gm.flags & WFLAG_END) {
+          // wake the epilogue on accumulator 0 only once every epilogue warp
+          // has taken its previous use: an earlier arrival would complete a
+          // second phase of dfull[0] under a warp still waiting for the
+          // first (parity aliasing)
+          wait_or_abort(&S.dfree[0], (use[0] & 1) ^ 1, abort_flag, T.wait_limit);
           mbar_arrive(&S.dfull[0]);
           break;
         }
