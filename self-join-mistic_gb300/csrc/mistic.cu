@@ -310,21 +310,21 @@ int bit_length(uint64_t v) {
   return b;
 }
 
-// Smallest home bin that goes to the tensor-core join.  MISTIC_TC_MIN_BIN
-// overrides it (tuning).
-// Smallest home bin joined on the tensor cores.  A tensor-core tile costs
-// about the same per candidate row whatever its number of home rows, a
-// CUDA-core unit costs d FMAs per cell, so small bins go to the CUDA cores
-// for short rows only.  Measured on GB300 (5M x 18: best 48-96; 515k x 90:
-// best 1-6): 20000 / d^2, clamped to [1, 64].
+// Smallest home bin joined on the tensor cores (MISTIC_TC_MIN_BIN overrides
+// it, for tuning).  A tensor-core tile costs about the same per candidate row
+// whatever its number of home rows, a CUDA-core unit costs d FMAs per cell,
+// so small bins go to the CUDA cores.  Measured on GB300 (whole join, ms):
+//   5M x 18:    T = 48: 150.2, 61: 147.0, 80: 145.2, 100: 145.1, 128: 146.8
+//   515k x 90:  T = 1: 259.9, 2: 261.9, 4: 261.9, 8: 263.3
+// hence 29000 / d^2, clamped to [1, 96].
 uint32_t tc_min_bin(uint32_t d) {
   const char* e = getenv("MISTIC_TC_MIN_BIN");
   if (e && *e) return (uint32_t)std::max(1l, strtol(e, nullptr, 10));
   // long rows (K-chunked kernel): a tile costs ~3 * 2 * 128 * d tensor flops
-  // per candidate column whatever its home rows, the FP32 CUDA cores 3 d
-  // per row and column, so bins of fewer than ~16 rows stay on the CUDA cores
-  if (join::tc_kp(d) > 128) return 16;
-  return (uint32_t)std::min(64.0, std::max(1.0, std::floor(20000.0 / ((double)d * d))));
+  // per candidate column whatever its home rows, the FP32 CUDA cores 3 d per
+  // row and column; measured on 2M x 384: T = 8: 1383, 16: 1422, 24: 1514 ms
+  if (join::tc_kp(d) > 128) return 8;
+  return (uint32_t)std::min(96.0, std::max(1.0, std::floor(29000.0 / ((double)d * d))));
 }
 
 void check_handle(mistic_handle h) {
