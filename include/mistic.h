@@ -240,8 +240,13 @@ const char* mistic_last_error(mistic_handle h);
  * MISTIC_NOALLOC_MAX_D; larger inputs are rejected with MISTIC_ERR_TOO_LARGE.
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current: make it before any stream
- * capture.  All calls share the array, so calls that overlap on the GPU (from
- * several streams or host threads) race; serialise them. */
+ * capture.  Under CUDA's default lazy module loading the array is allocated
+ * when the library's module first loads on the device, which is that first
+ * call: make it before a pool allocator reserves the device's memory (a call
+ * with n = 0 does only this set-up).  Inputs with a NaN or infinite
+ * coordinate are rejected with MISTIC_ERR_NOT_FINITE.  All calls share the
+ * array, so calls that overlap on the GPU (from several streams or host
+ * threads) race; serialise them. */
 #define MISTIC_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 #define MISTIC_NOALLOC_MAX_D 128u
 mistic_status mistic_selfjoin_noalloc(const void* d_pts, uint64_t n, uint32_t d, mistic_dtype dtype,

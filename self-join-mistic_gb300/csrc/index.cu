@@ -451,11 +451,36 @@ __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __rest
     ++nseg;
   }
   if (!FILL) {
+    // a bin's unit count saturates at 2^32 - 1; the 64-bit totals of the
+    // three count arrays (k_count_totals) then exceed the 32-bit offsets the
+    // work lists use, and the call fails with MISTIC_ERR_TOO_LARGE
+    const unsigned long long nu = (unsigned long long)nseg * nchunks;
+    const uint32_t nu32 = nu > 0xffffffffull ? 0xffffffffu : (uint32_t)nu;
     nbr_cnt[hb] = cnt;
-    unit_cnt[hb] = tc ? 0u : nseg * nchunks;
-    unit_cnt_tc[hb] = tc ? nseg * nchunks : 0u;
+    unit_cnt[hb] = tc ? 0u : nu32;
+    unit_cnt_tc[hb] = tc ? nu32 : 0u;
     cand[hb] = c;
   }
+}
+
+// 64-bit sums of the three per-bin count arrays of the enumeration (the
+// scans that turn them into offsets are 32-bit).
+__global__ void k_count_totals(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
+                               const uint32_t* __restrict__ c, uint32_t m, unsigned long long* __restrict__ tot) {
+  unsigned long long s[3] = {0, 0, 0};
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    s[0] += a[i];
+    s[1] += b[i];
+    s[2] += c[i];
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) s[k] += __shfl_xor_sync(FULL_MASK, s[k], o);
+  }
+  if ((threadIdx.x & 31) == 0)
+    for (int k = 0; k < 3; ++k)
+      if (s[k]) atomicAdd(&tot[k], s[k]);
 }
 
 // ------------------------------------------------------------ host launchers
@@ -553,6 +578,14 @@ void enumerate(mistic_handle_s* h, const uint64_t* bkey, const uint32_t* bstart,
     k_enum<true><<<nb, 128, 0, h->stream>>>(bkey, bstart, m, P, nullptr, nullptr, nullptr, nullptr, nbr_off,
                                             unit_off, unit_off_tc, nbr, units, units_tc);
   launched(h, fill ? "enum_fill" : "enum_count");
+}
+
+void count_totals(mistic_handle_s* h, const uint32_t* nbr_cnt, const uint32_t* unit_cnt, const uint32_t* unit_cnt_tc,
+                  uint32_t m, unsigned long long* tot) {
+  MCK(cudaMemsetAsync(tot, 0, 3 * sizeof(unsigned long long), h->stream));
+  const unsigned nb = std::max(1u, std::min((m + 255) / 256, 4u * (unsigned)h->sms));
+  k_count_totals<<<nb, 256, 0, h->stream>>>(nbr_cnt, unit_cnt, unit_cnt_tc, m, tot);
+  launched(h, "count_totals");
 }
 
 }  // namespace idx

@@ -225,6 +225,9 @@ void enumerate(mistic_handle_s*, const uint64_t* bkey, const uint32_t* bstart, u
                const EnumParams&, uint32_t* nbr_cnt, uint32_t* unit_cnt, uint32_t* unit_cnt_tc,
                unsigned long long* cand, const uint32_t* nbr_off, const uint32_t* unit_off,
                const uint32_t* unit_off_tc, uint32_t* nbr, Unit* units, Unit* units_tc, bool fill);
+// 64-bit totals of the enumeration's three per-bin count arrays into tot[3]
+void count_totals(mistic_handle_s*, const uint32_t* nbr_cnt, const uint32_t* unit_cnt, const uint32_t* unit_cnt_tc,
+                  uint32_t m, unsigned long long* tot);
 }  // namespace idx
 
 // ---- mistic.cu: FP32 filter thresholds (accept at or below t_lo, re-decide

@@ -462,6 +462,10 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     int fb[MAX_K];
     for (uint32_t j = 0; j < kk; ++j) {
       const double dmin = mmh[j], dmax = mmh[kk + j];
+      // distances that overflow FP64 (coordinates near 1e300) or a reference
+      // point that is not finite: the field cannot bin, so it is dropped and
+      // all points share it (the ±1 guarantee needs finite fields)
+      if (!std::isfinite(dmin) || !std::isfinite(dmax) || !(dmax >= dmin)) continue;
       const double u64 = ldexp(1.0, -53);
       const double ratio = eps > 0 ? dmax / eps : 0.0;
       const double delta = std::max(ldexp(1.0, -20), 8.0 * (d + 4) * u64 * (1.0 + ratio));
@@ -578,15 +582,29 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   idx::enumerate(h, bkey, bstart, m, ep, nbr_cnt, unit_cnt, unit_cnt_tc, cand, nullptr, nullptr, nullptr, nullptr,
                  nullptr, nullptr, false);
   uint32_t* tot32 = abuf<uint32_t>(h, "tot32", 3);
-  unsigned long long* tot64 = abuf<unsigned long long>(h, "tot64", 1);
+  unsigned long long* tot64 = abuf<unsigned long long>(h, "tot64", 4);
+  // 64-bit totals first: the work lists index neighbours and units with
+  // 32-bit offsets, which a total of 2^32 or more would wrap
+  idx::count_totals(h, nbr_cnt, unit_cnt, unit_cnt_tc, m, tot64 + 1);
   exclusive_scan<uint32_t>(h, nbr_cnt, nbr_cnt, m, tot32);
   exclusive_scan<uint32_t>(h, unit_cnt, unit_cnt, m, tot32 + 1);
   exclusive_scan<uint32_t>(h, unit_cnt_tc, unit_cnt_tc, m, tot32 + 2);
   exclusive_scan<unsigned long long>(h, cand, cand, m, tot64);
   uint32_t tots[3];
-  unsigned long long totc = 0;
+  unsigned long long tot_all[4] = {0, 0, 0, 0};
   d2h(h, tots, tot32, sizeof tots);
-  d2h(h, &totc, tot64, sizeof totc);
+  d2h(h, tot_all, tot64, sizeof tot_all);
+  const unsigned long long totc = tot_all[0];
+  {
+    // MISTIC_TEST_WORKLIST_LIMIT=k lowers the limit (tests of this check)
+    unsigned long long lim = 0xffffffffull - 1;
+    if (const char* e = getenv("MISTIC_TEST_WORKLIST_LIMIT")) lim = std::min(lim, strtoull(e, nullptr, 10));
+    for (int i = 0; i < 3; ++i)
+      if (tot_all[1 + i] > lim || tot_all[1 + i] != (unsigned long long)tots[i])
+        throw Error(MISTIC_ERR_TOO_LARGE,
+                    "neighbour-bin or work-unit list beyond the 32-bit offsets of the join work lists "
+                    "(raise eps resolution: more reference points, or split the input)");
+  }
   r->n_bin_pairs = tots[0];
   r->n_units = tots[1];
   r->n_units_tc = tots[2];
@@ -696,7 +714,11 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     jp.band_cap = bcap;
   }
   JoinCounters hc{};
-  for (int attempt = 0; attempt < 3; ++attempt) {
+  // MISTIC_TEST_JOIN_ATTEMPTS=k caps the passes (tests of the exit check below)
+  int attempts = 3;
+  if (const char* e = getenv("MISTIC_TEST_JOIN_ATTEMPTS")) attempts = std::max(1, atoi(e));
+  bool complete = false;
+  for (int attempt = 0; attempt < attempts; ++attempt) {
     MCK(cudaMemsetAsync(ctr, 0, 2 * sizeof(JoinCounters), h->stream));
     if (o.timing) MCK(cudaEventRecord(h->jev[0], h->stream));
     join::run(h, fp64, CH, jp);
@@ -711,12 +733,19 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
       jp.band_list = abuf<unsigned long long>(h, "band", jp.band_cap);
       continue;
     }
-    if (!need_pairs || hc.pairs <= cap || o.pair_capacity) break;
+    if (!need_pairs || hc.pairs <= cap || o.pair_capacity) {
+      complete = true;
+      break;
+    }
     cap = hc.pairs;
     pbuf = abuf<unsigned long long>(h, "pairs", cap);
     jp.pairs = pbuf;
     jp.cap = cap;
   }
+  // the last pass must have decided every band pair and, with a library-sized
+  // pair buffer, stored every pair; otherwise the counts are not a result
+  if (!complete)
+    throw Error(MISTIC_ERR_INTERNAL, "the join's band list or pair buffer still overflowed after its last pass");
   clk.mark();  // 7
   r->pairs_ij = hc.pairs;
   r->pairs_ordered_incl_self = 2 * hc.pairs + n;

@@ -23,6 +23,13 @@
 // call on each device looks the device address up with cudaGetSymbolAddress
 // (with that device current), checks the result and caches it; kernels get
 // that pointer.  Make the first call on a device before any stream capture.
+// Under CUDA's default lazy module loading the array itself is only
+// allocated when this module first loads on a device, i.e. at that first
+// call: make it (a call with n = 0 does only the set-up) before a pool
+// allocator reserves the device's memory.
+//
+// Inputs holding a NaN or an infinite coordinate are rejected with
+// MISTIC_ERR_NOT_FINITE, as mistic_selfjoin does by default.
 //
 // Every call shares the one scratch block and it keeps the previous call's
 // contents: each call clears the counters it relies on before use.  Calls
@@ -53,6 +60,7 @@ struct NaHeader {
   unsigned long long band;
   unsigned long long next_unit;
   unsigned long long r2max_bits;  // largest squared FP32 row norm, as FP64 bits
+  unsigned long long nonfinite;   // non-zero: an input coordinate is NaN or infinite
 };
 
 struct NaParams {
@@ -62,6 +70,7 @@ struct NaParams {
   const float* xf;  // FP32 rows relative to row 0, in the scratch
   NaHeader* hdr;    // in the scratch
   float t_lo, t_hi;
+  int all_fp64;     // 1: FP32 cannot separate the pairs; every candidate is decided in FP64
   double eps2;
   unsigned long long* pairs;  // caller's buffer, packed (i << 32 | j)
   unsigned long long cap;
@@ -73,20 +82,27 @@ __device__ __forceinline__ double na_ld(const void* p, int f32, size_t i) {
   return f32 ? (double)((const float*)p)[i] : ((const double*)p)[i];
 }
 
-// FP32 copy of every row minus row 0 (zero padded to dpad) and the largest
-// squared row norm.
+// FP32 copy of every row minus row 0 (zero padded to dpad), the largest
+// squared row norm, and a flag for NaN or infinite input coordinates (one
+// such value in row 0 would otherwise poison every FP32 row).
 __global__ void k_na_convert(NaParams P) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   double r2 = 0.0;
+  bool bad = false;
   if (i < P.n) {
     float* row = const_cast<float*>(P.xf) + (size_t)i * P.dpad;
     for (uint32_t t = 0; t < P.dpad; ++t) {
       float v = 0.f;
-      if (t < P.d) v = (float)(na_ld(P.raw, P.raw_f32, (size_t)i * P.d + t) - na_ld(P.raw, P.raw_f32, t));
+      if (t < P.d) {
+        const double xi = na_ld(P.raw, P.raw_f32, (size_t)i * P.d + t);
+        bad |= !isfinite(xi);
+        v = (float)(xi - na_ld(P.raw, P.raw_f32, t));
+      }
       row[t] = v;
       r2 = fma((double)v, (double)v, r2);
     }
   }
+  if (__any_sync(FULL_MASK, bad) && (threadIdx.x & 31) == 0) atomicExch(&P.hdr->nonfinite, 1ull);
 #pragma unroll
   for (int o = 16; o; o >>= 1) r2 = fmax(r2, __shfl_xor_sync(FULL_MASK, r2, o));
   if ((threadIdx.x & 31) == 0 && r2 > 0.0)
@@ -157,10 +173,16 @@ __global__ void __launch_bounds__(kThreads) k_na_join(const NaParams P) {
         }
       }
       uint32_t m = 0, lo = 0;
+      if (P.all_fp64) {
+        // the FP32 values are not usable (an offset beyond FLT_MAX is inf and
+        // inf - inf is NaN): every candidate goes to the FP64 decision
+        m = FULL_MASK;
+      } else {
 #pragma unroll
-      for (int a = 0; a < kCH; ++a) {
-        m |= (acc[a] <= P.t_hi ? 1u : 0u) << a;
-        lo |= (acc[a] <= P.t_lo ? 1u : 0u) << a;
+        for (int a = 0; a < kCH; ++a) {
+          m |= (acc[a] <= P.t_hi ? 1u : 0u) << a;
+          lo |= (acc[a] <= P.t_lo ? 1u : 0u) << a;
+        }
       }
       // valid home rows: a < na and a0 + a < q
       uint32_t valid = na >= 32 ? FULL_MASK : ((1u << na) - 1u);
@@ -252,10 +274,12 @@ extern "C" mistic_status mistic_selfjoin_noalloc(const void* d_pts, uint64_t n, 
   if (d > MISTIC_NOALLOC_MAX_D || n >= 0xffffffffull ||
       (unsigned long long)n * dpad * sizeof(float) > kScratchBytes - kHeaderBytes)
     return MISTIC_ERR_TOO_LARGE;
-  if (n < 2) return MISTIC_OK;
+  // set-up first, even for n < 2: a call with n = 0 only resolves the
+  // scratch array on the current device (see the header)
   void* scratch = nullptr;
   mistic_status st = scratch_address(&scratch);
   if (st != MISTIC_OK) return st;
+  if (n < 2) return MISTIC_OK;
   cudaStream_t s = (cudaStream_t)stream;
   NaParams P{};
   P.raw = d_pts;
@@ -275,13 +299,15 @@ extern "C" mistic_status mistic_selfjoin_noalloc(const void* d_pts, uint64_t n, 
   NaHeader hh{};
   if ((st = cuda_status(cudaMemcpyAsync(&hh, P.hdr, sizeof hh, cudaMemcpyDeviceToHost, s))) != MISTIC_OK) return st;
   if ((st = cuda_status(cudaStreamSynchronize(s))) != MISTIC_OK) return st;
+  if (hh.nonfinite) return MISTIC_ERR_NOT_FINITE;
   double r2 = 0.0;
   memcpy(&r2, &hh.r2max_bits, sizeof r2);
   const double R = sqrt(r2) * (1.0 + 1e-12);
   const double eps2 = P.eps2;
-  if (eps2 == 0.0 || eps2 < 1e-28 || R > 1e15 || !filter_thresholds(d, eps2, R, &P.t_lo, &P.t_hi)) {
+  if (eps2 == 0.0 || eps2 < 1e-28 || !(R <= 1e15) || !filter_thresholds(d, eps2, R, &P.t_lo, &P.t_hi)) {
     P.t_lo = -1.0f;  // FP32 cannot separate these pairs: re-decide every candidate in FP64
     P.t_hi = INFINITY;
+    P.all_fp64 = 1;
   }
   const uint32_t nchunks = (uint32_t)((n + kCH - 1) / kCH);
   P.nseg = (uint32_t)((n + kSeg - 1) / kSeg);

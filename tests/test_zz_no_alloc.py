@@ -69,3 +69,81 @@ def test_noalloc_limits_and_overflow(handle):
                                        ctypes.byref(cnt), None) == L.ERR_TOO_LARGE
     assert lib.mistic_selfjoin_noalloc(ctypes.c_void_p(xt.data_ptr()), 10, L.NOALLOC_MAX_D + 1, L.F64, 0.1,
                                        None, 0, ctypes.byref(cnt), None) == L.ERR_TOO_LARGE
+
+
+def _pairs_of(buf, cnt):
+    got = buf[:cnt].cpu().numpy().view(np.uint32).reshape(-1, 2)
+    assert (got[:, 0] < got[:, 1]).all()
+    return canon(got)
+
+
+@pytest.mark.parametrize("case", ["max_d", "tiny_eps", "huge_offsets"])
+def test_noalloc_edge_cases_against_oracle(handle, case):
+    """d at MISTIC_NOALLOC_MAX_D, and the two inputs on which the FP32 filter
+    cannot be used (eps^2 below 1e-28; row offsets beyond FLT_MAX), where every
+    candidate is decided in FP64: the pair set must equal the oracle's and the
+    regular entry point's."""
+    torch = pytest.importorskip("torch")
+    from oracle import oracle as O
+    lib = L.load()
+    rng = np.random.default_rng(11)
+    if case == "max_d":
+        d = int(L.NOALLOC_MAX_D)
+        x = rng.random((1500, d))
+        x[700:710] = x[0:10] + 1e-3  # a few close pairs
+        eps = 0.05
+    elif case == "tiny_eps":
+        d = 5
+        x = rng.random((2000, d))
+        x[1000:1040] = x[0:40]  # exact duplicates: distance 0
+        eps = 1e-15
+    else:
+        d = 3
+        x = rng.random((2000, d))
+        x[100:120] = 1e300  # twenty identical far rows, row 0 near the origin
+        eps = 0.02
+    ref = O.brute_pairs(x, eps)
+    assert len(ref) > 0
+    assert np.array_equal(handle.selfjoin(x, 4, eps, pairs="host", sort_pairs=True).pairs, ref)
+    xt = torch.from_numpy(x).cuda()
+    for _ in range(2):
+        st, cnt, buf = _noalloc(lib, torch, xt, x.shape[0], d, L.F64, eps, len(ref) + 16)
+        assert st == L.OK, lib.mistic_strerror(st)
+        assert cnt == len(ref)
+        assert np.array_equal(_pairs_of(buf, cnt), ref)
+
+
+def test_noalloc_rejects_non_finite_and_allocates_nothing(handle):
+    """A NaN in row 0 (which every FP32 row is taken relative to) is rejected
+    as the regular entry point rejects it; and a second call leaves the
+    device's free memory exactly where the first left it."""
+    torch = pytest.importorskip("torch")
+    from oracle import oracle as O
+    lib = L.load()
+    x = np.random.default_rng(5).random((4000, 18))
+    eps = 0.75
+    ref = O.brute_pairs(x, eps)
+    xt = torch.from_numpy(x).cuda()
+    buf = torch.zeros((len(ref) + 16,), dtype=torch.int64, device="cuda")
+    cnt = ctypes.c_uint64(0)
+
+    def call(pts):
+        torch.cuda.synchronize()
+        return lib.mistic_selfjoin_noalloc(ctypes.c_void_p(pts.data_ptr()), x.shape[0], 18, L.F64, eps,
+                                           ctypes.c_void_p(buf.data_ptr()), len(ref) + 16, ctypes.byref(cnt),
+                                           None)
+
+    assert call(xt) == L.OK and cnt.value == len(ref)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    assert call(xt) == L.OK and cnt.value == len(ref)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert np.array_equal(_pairs_of(buf, cnt.value), ref)
+    bad = xt.clone()
+    bad[0, 3] = float("nan")
+    assert call(bad) == L.ERR_NOT_FINITE
+    import mistic
+    with pytest.raises(mistic.MisticError) as ei:
+        handle.selfjoin(bad.cpu().numpy(), 6, eps)
+    assert ei.value.status == L.ERR_NOT_FINITE
