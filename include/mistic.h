@@ -210,6 +210,16 @@ mistic_status mistic_bruteforce_rows(mistic_handle h, const void* pts, uint64_t 
  * the number of values written (may be NULL).  Host only; needs no GPU. */
 mistic_status mistic_convert_text(const char* text_path, const char* bin_path, uint64_t* out_count);
 
+/* Diagnostic with no counterpart in the reference: one 128 x 128 tensor-core
+ * Gram tile D = A B^T (tcgen05.mma, FP32 accumulation in tensor memory,
+ * issued exactly as the joins issue it), for measuring the accumulation error
+ * that the joins' band bound allows for.  kind 0: a and b are 128 x K bf16
+ * bit patterns (uint16, row-major, K a multiple of 16, K <= 256); kind 1:
+ * 128 x K FP32 values read as tf32 (K a multiple of 8, K <= 128).  d receives
+ * the 128 x 128 FP32 tile, row-major.  All pointers are host memory; runs on
+ * the current device and returns when done. */
+mistic_status mistic_tc_gram_probe(int kind, const void* a, const void* b, uint32_t K, float* d);
+
 /* Release the buffers a result owns (pair list).  Safe on a zeroed result. */
 void mistic_result_free(mistic_result* r);
 

@@ -30,6 +30,7 @@ EXPORTS = (
     "mistic_selfjoin", "mistic_batch_selfjoin", "mistic_read_points",
     "mistic_free_host", "mistic_result_free", "mistic_strerror",
     "mistic_last_error", "mistic_selfjoin_noalloc", "mistic_convert_text", "mistic_bruteforce_rows",
+    "mistic_tc_gram_probe",
 )
 
 #: scratch limits of mistic_selfjoin_noalloc (include/mistic.h)
@@ -144,5 +145,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
     L.mistic_selfjoin_noalloc.argtypes = [vp, u64, u32, ctypes.c_int, dbl, vp, u64,
                                           ctypes.POINTER(u64), vp]
     L.mistic_selfjoin_noalloc.restype = ctypes.c_int
+    L.mistic_tc_gram_probe.argtypes = [ctypes.c_int, vp, vp, u32, vp]
+    L.mistic_tc_gram_probe.restype = ctypes.c_int
     _lib = L
     return L

@@ -22,7 +22,7 @@ PEAKS = os.path.join(BUILD, "mistic_peaks")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC"] + ARCH
-LIB_CU = ["sort.cu", "index.cu", "join.cu", "join_tc.cu", "join_tcw.cu", "mistic.cu", "noalloc.cu", "brute.cu"]
+LIB_CU = ["sort.cu", "index.cu", "join.cu", "join_tc.cu", "join_tcw.cu", "mistic.cu", "noalloc.cu", "brute.cu", "probe.cu"]
 LIB_CPP = ["rp.cpp", "io.cpp"]
 
 
