@@ -19,9 +19,15 @@ written), i.e. the work the reference's nodeLauncher5 does per dataset.
 Also reported: wall time per join, distance evaluations/s (unordered
 candidate pairs the join evaluated / step time), pairs/s, the plain FP64
 CUDA-core join on the same index (identical pair set required), the roofline
-of the dominant kernel and a CPU baseline (the reference's brute-force
-algorithm, src/utils.cu:285-317, as the oracle's C port, on a bounded row
-sample, extrapolated to the whole job).
+of the dominant kernel, the whole step against its lower bound, and a CPU
+baseline (the reference's brute-force algorithm, src/utils.cu:285-317, as
+the oracle's C port, on a bounded row sample, extrapolated to the whole job).
+
+The line also carries the benchmark spec: the 5M x 384 clustered FP32 workload
+(TINY-shaped, k = 8, 16 mean neighbours) measured in the same run -- mixed
+precision at full size, and mixed precision against the plain FP64 join
+(and TF32) on a fixed full-density sample of home points (mistic_opts.
+home_sample), with the pair sets compared bit for bit.
 
 `--impl reference` times that CPU implementation alone (rank 0 only).
 """
@@ -77,18 +83,16 @@ WORKLOADS = {
               "MSD-shaped n=515,345 d=90 FP64, k=8, 16 mean neighbours"),
     # ε calibrated on each generated set (drawn on the GPU at this size)
     "tiny384": (lambda n: W.tiny384(n or 5_000_000),
-                "TINY-shaped n=5e6 d=384 FP32, 1000 Zipf clusters, L2-normalised, k=8, 16 mean neighbours"),
+                "TINY-shaped n=5e6 d=384 FP32, 1000 Zipf(1.1) clusters with full-rank covariance "
+                "(eigenvalues log-uniform in [1e-3,1]), L2-normalised, k=8, 16 mean neighbours"),
 }
 
 FALLBACK_PEAKS = {"hbm_gbs": 6785.9, "bf16_tflops": 1922.1, "bf16_tflops_sustained": 1711.2}
 
 #: DRAM bytes (read + write) per evaluated cell of k_join_tc on the SUSY-shaped
-#: data, from the ncu capture of the 2.5M-point case (profiles/join_tc_susy18.md:
-#: 283.8 MB over 2.1993e10 cells); scaled by the cells of the measured launch.
+#: data, from an ncu capture of the 2.5M-point case (283.8 MB over 2.1993e10
+#: cells); scaled by the cells of the measured launch.
 TC_DRAM_BYTES_PER_CELL_SUSY18 = 283.8e6 / 2.1993e10
-#: the same for k_join_tcw on the TINY-shaped data, from the capture of the
-#: 300k-point case (profiles/join_tcw_tiny384.md: 20.507 GB over 1.4457e10 cells)
-TCW_DRAM_BYTES_PER_CELL_TINY384 = 20.507e9 / 1.4457096836e10
 
 
 def load_peaks() -> dict:
@@ -205,6 +209,14 @@ def job_points_per_s(n_per_rank: int, world: int, ms: float) -> float:
     return world * n_per_rank / (ms * 1e-3)
 
 
+def config_for(args, wl, world: int) -> dict:
+    """The `config` of the line: the same dict in both arms."""
+    return {"workload": args.workload, "n": wl.n, "d": wl.d, "k": wl.k, "eps_hex": float(wl.eps).hex(),
+            "desc": WORKLOADS[args.workload][1], "parallelism": "replicas" if world > 1 else "single",
+            "l2": f"inputs larger than L2 ({wl.n * wl.d * wl.pts.itemsize / 1e6:.0f} MB points per step)",
+            "pairs_to": "caller device buffer"}
+
+
 def run_reference(args, wl) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
@@ -221,8 +233,7 @@ def run_reference(args, wl) -> None:
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": job * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "n": wl.n, "d": wl.d, "k": wl.k,
-                   "eps_hex": float(wl.eps).hex(), "desc": WORKLOADS[args.workload][1]},
+        "config": config_for(args, wl, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": samples[0]["threads"], "kind": "port",
                          "sample": f"rows [0,{samples[0]['rows']}) x all {wl.n} rows per step, "
                                    "extrapolated to n rows; brute_force of src/utils.cu:285-317 "
@@ -387,12 +398,8 @@ def run_mistic(args, wl) -> None:
                 "issued_tflops": r.tc_tiles * 128 * 128 * 3 * 2.0 * kmma / (tc_ms * 1e-3) / 1e12}
         if args.workload == "susy18":
             roof["traffic"] = TC_DRAM_BYTES_PER_CELL_SUSY18 * r.tc_cells
-            roof["traffic_source"] = ("ncu dram__bytes_read+write per cell of the 2.5M-point capture "
-                                      "(profiles/join_tc_susy18.md) x this launch's cells")
-        elif args.workload == "tiny384" and wide:
-            roof["traffic"] = TCW_DRAM_BYTES_PER_CELL_TINY384 * r.tc_cells
-            roof["traffic_source"] = ("ncu dram__bytes_read+write per cell of the 300k-point capture "
-                                      "(profiles/join_tcw_tiny384.md) x this launch's cells")
+            roof["traffic_source"] = ("ncu dram__bytes_read+write per cell of a 2.5M-point capture of the "
+                                      "same kernel x this launch's cells")
     else:
         # dominant kernel: the FP32 filter join; 3*d flops per candidate pair
         # (d subtractions, d multiply-adds) on the CUDA-core FP32 pipe
@@ -404,17 +411,16 @@ def run_mistic(args, wl) -> None:
                 "work": "3*d FP32 flops per candidate pair", "kernel_ms": simt_ms,
                 "peak_source": "mistic_peaks FFMA probe, this run (CUDA-core FP32 pipe)"}
     roof["hbm_peak_gbs"] = peaks.get("hbm_gbs")
+    step_roof = step_lower_bound(r, n, d, wl.k, ms, peaks)
+    north = None if (args.no_c5 or args.workload == "tiny384") else run_north_star(h, args, dev, stream, peaks)
     cpu = cpu_sample(x, wl.eps, args.cpu_seconds) if not args.no_cpu else None
     value = job_points_per_s(n, world, ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "n": n, "d": d, "k": wl.k, "eps_hex": float(wl.eps).hex(),
-                   "desc": WORKLOADS[args.workload][1], "mode": r.mode_used,
-                   "parallelism": "replicas" if world > 1 else "single",
-                   "l2": f"inputs larger than L2 ({n * d * x.itemsize / 1e6:.0f} MB points per step)",
-                   "pairs_to": "caller device buffer"},
+        "config": config_for(args, wl, world),
+        "mode_used": r.mode_used, "tc_operands": r.tc_operands,
         "pairs_ij": r.pairs_ij, "pairs_ordered_incl_self": r.pairs_ordered_incl_self,
         "candidates": r.candidates, "band_pairs": r.band_pairs, "ulp_ambiguous": r.ulp_ambiguous,
         "band_fraction": r.band_pairs / max(1, r.candidates),
@@ -426,6 +432,8 @@ def run_mistic(args, wl) -> None:
         "fp64_plain": fp64,
         "verify": verify,
         "roofline": roof,
+        "step_roofline": step_roof,
+        "north_star": north,
         "e2e": {"value": job_points_per_s(n, world, e2e_ms), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": n * d * x.itemsize, "d2h_bytes_per_step": int(r.pairs_ij) * 8,
                 "h2d_ms": statistics.mean(t[1] for t in e2e_res), "d2h_ms": statistics.mean(t[2] for t in e2e_res)},
@@ -439,6 +447,119 @@ def run_mistic(args, wl) -> None:
     }
     print(json.dumps(line), flush=True)
     h.close()
+
+
+def step_lower_bound(r, n: int, d: int, k: int, ms: float, peaks: dict) -> dict:
+    """The whole step against its lower bound: T_lb = index bytes / HBM +
+    max(join tensor flops / BF16, pair bytes / HBM), with 8d + s d + 3 (4k + 4)
+    index bytes a point (FP64 read for the reference-point distances, one
+    read in the join's dtype, key write plus one sort pass), 2 ceil16(d)
+    tensor flops per candidate pair, 8 bytes per result pair."""
+    hbm = peaks["hbm_gbs"] * 1e9
+    bf16 = peaks["bf16_tflops"] * 1e12
+    idx_bytes = n * (8 * d + 4 * d + 3 * (4 * k + 4))
+    join_flops = r.candidates * 2.0 * ((d + 15) // 16 * 16)
+    out_bytes = r.pairs_ij * 8.0
+    t_lb = idx_bytes / hbm + max(join_flops / bf16, out_bytes / hbm)
+    return {"t_lb_ms": t_lb * 1e3, "frac": t_lb * 1e3 / ms, "index_bytes": idx_bytes,
+            "join_tensor_flops": join_flops, "pair_bytes": out_bytes,
+            "model": "index bytes/HBM + max(2*ceil16(d) flops per candidate / BF16, 8 B per pair / HBM)"}
+
+
+def run_north_star(h, args, dev, stream, peaks) -> dict:
+    """The 5M x 384 clustered FP32 workload in the same run: mixed precision
+    at full size (args.c5_steps timed steps after one warm-up), then mixed
+    precision, plain FP64 and TF32 on one full-density sample of home points
+    (mistic_opts.home_sample, about 1.5e10 candidate pairs), pair sets
+    compared on the device."""
+    import torch
+    from mistic import _lib as L
+    t0 = time.perf_counter()
+    wl = W.tiny384(args.c5_n or 5_000_000)
+    gen_s = time.perf_counter() - t0
+    x = np.ascontiguousarray(wl.pts)
+    n, d = x.shape
+    xt = torch.from_numpy(x).to(dev)
+    del x
+    torch.cuda.synchronize()
+
+    def call(opts, m=n):
+        return h.to_result(h.selfjoin_raw(xt.data_ptr(), m, d, L.F32, wl.k, wl.eps, opts))
+
+    r0 = call(h.opts(input_on_device=True))
+    cap = int(r0.pairs_ij * 1.02) + 1024
+    pbuf = torch.empty((cap,), dtype=torch.int64, device=dev)
+    o_dev = h.opts(input_on_device=True, pairs="device", pair_capacity=cap, pair_buffer=pbuf.data_ptr())
+    call(o_dev)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    res = [call(o_dev) for _ in range(args.c5_steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.c5_steps
+    r = res[-1]
+    tc_ms = statistics.mean(q.ms["join_tc"] for q in res)
+    kd = {"split-bf16": (d + 31) // 32 * 32, "bf16": (d + 63) // 64 * 64, "tf32": (d + 31) // 32 * 32}.get(
+        r.tc_operands, d)
+    products = 3 if r.tc_operands == "split-bf16" else 1
+    tflops_2d = r.tc_cells * 2.0 * d / (tc_ms * 1e-3) / 1e12
+    issued = r.tc_tiles * 128 * 128 * products * 2.0 * kd / (tc_ms * 1e-3) / 1e12
+    tf32_scale = 2.0 if r.tc_operands == "tf32" else 1.0  # tf32 MMAs run at half the bf16 rate
+    roof = {"bound": "tensor", "kernel": "k_join_tcw", "operands": r.tc_operands, "achieved": tflops_2d,
+            "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": tflops_2d / peaks["bf16_tflops"],
+            "issued_tflops": issued, "issued_frac": issued * tf32_scale / peaks["bf16_tflops"],
+            "kernel_ms": tc_ms, "cells": r.tc_cells,
+            "work": "2*d flops per evaluated cell; issued = tiles x 128 x 128 x products x 2 x K"}
+    # ---- the same full-density sample in every mode
+    S = max(1, int(round(r.candidates / args.c5_sample_cands)))
+    cap_s = max(1 << 20, int(r.pairs_ij / max(1, S) * 4) + 4096)
+    bufs = {}
+    out = {}
+    for mode in ("auto", "fp64", "tf32"):
+        bufs[mode] = torch.empty((cap_s,), dtype=torch.int64, device=dev)
+        o = h.opts(input_on_device=True, pairs="device", pair_capacity=cap_s, pair_buffer=bufs[mode].data_ptr(),
+                   sort_pairs=True, mode=mode, home_sample=S)
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        q = call(o)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        out[mode] = (q, a0.elapsed_time(a1))
+    qa, qf, qt = out["auto"][0], out["fp64"][0], out["tf32"][0]
+    same = (qa.pairs_ij == qf.pairs_ij == qt.pairs_ij and
+            bool(torch.equal(bufs["auto"][:qa.pairs_ij], bufs["fp64"][:qf.pairs_ij])) and
+            bool(torch.equal(bufs["tf32"][:qt.pairs_ij], bufs["fp64"][:qf.pairs_ij])))
+    fp64_full_ms = qf.ms["join"] * r.candidates / max(1, qf.candidates) + (r.ms["total"] - r.ms["join"])
+    line = {
+        "workload": "tiny384", "n": n, "d": d, "k": wl.k, "eps_hex": float(wl.eps).hex(),
+        "desc": WORKLOADS["tiny384"][1], "generation_s": gen_s,
+        "steps": args.c5_steps, "warmup": 1, "ms_per_step": ms, "value": n / (ms * 1e-3), "unit": UNIT,
+        "mode_used": r.mode_used, "tc_operands": r.tc_operands,
+        "pairs_ij": r.pairs_ij, "candidates": r.candidates, "band_pairs": r.band_pairs,
+        "band_fraction": r.band_pairs / max(1, r.candidates), "ulp_ambiguous": r.ulp_ambiguous,
+        "distance_evals_per_s": r.candidates / (ms * 1e-3), "pairs_per_s": r.pairs_ij / (ms * 1e-3),
+        "phase_ms": {k2: round(v, 3) for k2, v in r.ms.items()},
+        "bins": r.n_bins, "units_tc": r.n_units_tc, "tc_tiles": r.tc_tiles,
+        "roofline": roof,
+        "sample": {
+            "home_sample": S, "candidates": qf.candidates, "pairs_ij": qf.pairs_ij,
+            "identical_pair_set_mixed_fp64_tf32": same,
+            "mixed": {"join_ms": qa.ms["join"], "step_ms": out["auto"][1], "band_pairs": qa.band_pairs,
+                      "tc_operands": qa.tc_operands},
+            "fp64": {"join_ms": qf.ms["join"], "step_ms": out["fp64"][1]},
+            "tf32": {"join_ms": qt.ms["join"], "step_ms": out["tf32"][1], "band_pairs": qt.band_pairs,
+                     "band_fraction": qt.band_pairs / max(1, qt.candidates)},
+            "mixed_vs_fp64_join": qf.ms["join"] / max(1e-9, qa.ms["join"]),
+            "note": "home points of about 1 in S groups of 512 sorted points per bin, each joined with all "
+                    "its candidates, identical in every mode; join_ms from the library's CUDA events"},
+        "fp64_full_ms_extrapolated": fp64_full_ms,
+        "mixed_vs_fp64_full_step": fp64_full_ms / ms,
+    }
+    del xt, pbuf, bufs
+    torch.cuda.empty_cache()
+    return line
 
 
 def run_batch(args) -> None:
@@ -597,6 +718,11 @@ def main() -> None:
                     help="check the neighbour counts of this many rows against the GPU FP64 brute force")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-c5", action="store_true", help="skip the 5M x 384 north-star measurement")
+    ap.add_argument("--c5-n", type=int, default=0, help="points of the north-star workload (default 5,000,000)")
+    ap.add_argument("--c5-steps", type=int, default=2, help="timed full-size steps of the north-star workload")
+    ap.add_argument("--c5-sample-cands", type=float, default=1.5e10,
+                    help="candidate pairs of the north-star mixed/FP64 sample")
     ap.add_argument("--ref-seconds", type=float, default=6.0)
     args = ap.parse_args()
     if args.workload == "batch2000":

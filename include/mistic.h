@@ -71,9 +71,17 @@ typedef enum mistic_mode {
   MISTIC_MODE_AUTO = 0, /* BF16 tensor-core mode for 8 <= d <= 126, else the FP32 filter */
   MISTIC_MODE_FP64 = 1, /* plain FP64 CUDA-core distances for every candidate */
   MISTIC_MODE_FP32 = 2, /* FP32 CUDA-core filter + FP64 re-decision of the band */
-  MISTIC_MODE_BF16 = 3  /* large home bins as split-BF16 tensor-core Gram tiles (FP32
-                           accumulation, d + 2 <= 128), small ones on the FP32 filter;
-                           FP64 re-decision of the band in both */
+  MISTIC_MODE_BF16 = 3, /* large home bins as BF16 tensor-core Gram tiles (FP32
+                           accumulation): split hi/lo operands, or, for long rows
+                           (d + 2 > 128) when the bound leaves a narrow band, single
+                           BF16 operands; small bins on the FP32 filter; FP64
+                           re-decision of the band in both */
+  MISTIC_MODE_TF32 = 4  /* large home bins as TF32 tensor-core Gram tiles (kind::tf32,
+                           rows rounded to TF32 once, globally centred, FP32
+                           accumulation), small bins on the FP32 filter; FP64
+                           re-decision of the band.  Columns whose TF32 bound exceeds
+                           eps^2 / 10 (small eps against the rows' norms) are decided
+                           entirely in FP64, so BF16 is the faster choice there */
 } mistic_mode;
 
 typedef enum mistic_rp_mode {
@@ -109,6 +117,14 @@ typedef struct mistic_opts {
   mistic_pairs_where csr;     /* per-point neighbour table (CSR), the reference's neighborTable
                                  (include/utils.cuh:33-41, built in src/launcher.cu:4-50):
                                  NONE (default), HOST or DEVICE; see mistic_result.csr_* */
+  uint32_t home_sample;       /* 0 or 1 (default): join every point.  S > 1: a sample at
+                                 full density -- only the points of about 1 in S groups
+                                 of 512 consecutive points of each bin's sorted order
+                                 (picked by a hash of bin and group, the same in every
+                                 mode) are joined as home points, each against all its
+                                 candidates; counts, pair list and times cover that
+                                 sample.  For comparing modes and tuning on a fixed
+                                 subset of the work.  No counterpart in the reference. */
 } mistic_opts;
 
 typedef struct mistic_result {
@@ -140,6 +156,8 @@ typedef struct mistic_result {
   uint64_t* csr_offsets;            /* n + 1 entries */
   uint32_t* csr_nbrs;               /* csr_offsets[n] entries */
   int32_t csr_on_device;
+  int32_t tc_operands;              /* tensor-core operand precision used: 0 none, 1 split
+                                       bf16 (hi/lo), 2 single bf16, 3 tf32 */
   void* _owner;                     /* internal: non-NULL when the result owns `pairs` */
 } mistic_result;
 

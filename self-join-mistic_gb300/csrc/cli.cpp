@@ -12,7 +12,7 @@
 //
 // Options (none exist in the reference):
 //   --f32              input file holds FP32 rows
-//   --mode auto|fp64|fp32
+//   --mode auto|fp64|fp32|bf16|tf32
 //   --rp pca|box       reference-point placement
 //   --seed S
 //   --pairs out.bin    write the i<j pair list as uint32 (i, j) rows, sorted
@@ -32,7 +32,7 @@
 
 static int usage(const char* p) {
   fprintf(stderr,
-          "usage: %s <file.bin> <dim> <numRP> <epsilon> [--f32] [--mode auto|fp64|fp32] "
+          "usage: %s <file.bin> <dim> <numRP> <epsilon> [--f32] [--mode auto|fp64|fp32|bf16|tf32] "
           "[--rp pca|box] [--seed S] [--pairs out.bin] [--device N]\n"
           "       %s --to-bin <in.txt> <out.bin>\n",
           p, p);
@@ -70,7 +70,11 @@ int main(int argc, char** argv) {
       const char* v = next();
       if (!v) return usage(argv[0]);
       std::string m = v;
-      o.mode = m == "fp64" ? MISTIC_MODE_FP64 : m == "fp32" ? MISTIC_MODE_FP32 : MISTIC_MODE_AUTO;
+      o.mode = m == "fp64"   ? MISTIC_MODE_FP64
+               : m == "fp32" ? MISTIC_MODE_FP32
+               : m == "bf16" ? MISTIC_MODE_BF16
+               : m == "tf32" ? MISTIC_MODE_TF32
+                             : MISTIC_MODE_AUTO;
     } else if (a == "--rp") {
       const char* v = next();
       if (!v) return usage(argv[0]);

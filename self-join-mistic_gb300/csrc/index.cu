@@ -350,6 +350,20 @@ __device__ __forceinline__ uint32_t lower_bound_u64(const uint64_t* __restrict__
   return lo;
 }
 
+// Home-point sample (mistic_opts.home_sample): group g (points
+// [512 g, 512 g + 512) of bin h's sorted order) takes part iff a hash of
+// (h, g) is 0 mod S.  Every unit chunk size (4 .. 512 points) divides 512,
+// so a unit is either wholly in the sample or wholly out of it, in every mode.
+constexpr uint32_t SAMPLE_GROUP = 512;
+__device__ __forceinline__ bool group_sampled(uint32_t h, uint32_t g, uint32_t S) {
+  if (S <= 1) return true;
+  uint32_t x = h * 0x9E3779B1u ^ (g + 0x7F4A7C15u) * 0x85EBCA77u;
+  x ^= x >> 15;
+  x *= 0x2C1B3C6Du;
+  x ^= x >> 12;
+  return x % S == 0;
+}
+
 template <bool FILL>
 __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __restrict__ bstart,
                        uint32_t m, EnumParams P, uint32_t* __restrict__ nbr_cnt,
@@ -366,6 +380,21 @@ __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __rest
   const uint32_t csz = tc ? P.tc_chunk : P.chunk;
   const uint32_t nchunks = (asz + csz - 1) / csz;
   Unit* __restrict__ units = tc ? units_tc : units_simt;
+  // sampled home points: chunks taken, home points and their pairs inside the bin
+  uint32_t nchunks_s = nchunks;
+  unsigned long long rows_s = asz, self_s = (unsigned long long)asz * (asz - (asz > 0)) / 2;
+  if (P.sample > 1) {
+    nchunks_s = 0;
+    for (uint32_t ch = 0; ch < nchunks; ++ch) nchunks_s += group_sampled(hb, ch * csz / SAMPLE_GROUP, P.sample);
+    rows_s = 0;
+    self_s = 0;
+    for (uint32_t g0 = 0; g0 < asz; g0 += SAMPLE_GROUP) {
+      if (!group_sampled(hb, g0 / SAMPLE_GROUP, P.sample)) continue;
+      const unsigned long long g1 = min(asz, g0 + SAMPLE_GROUP), c = g1 - g0;
+      rows_s += c;
+      self_s += c * (asz - 1) - (g0 + g1 - 1) * c / 2;  // pairs (p, q) of the bin with p in the group, q > p
+    }
+  }
 
   int kf[MAX_K];
   // decode fields: field j spans [shift[j], shift[j-1]) (shift[-1] = 64)
@@ -394,11 +423,12 @@ __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __rest
   // split and, in pass 2, the neighbour list and the units.
   auto leaf = [&](uint32_t a) {
     const uint32_t bsz = bstart[a + 1] - bstart[a];
-    c += (a == hb) ? (unsigned long long)asz * (asz - 1) / 2 : (unsigned long long)asz * bsz;
+    c += (a == hb) ? self_s : rows_s * bsz;
     if (seg_fill > 0 && seg_fill + bsz > P.seg_cap) {
       if (FILL) {
         for (uint32_t ch = 0; ch < nchunks; ++ch)
-          units[w_unit++] = Unit{hb, ch, nbr_off[hb] + seg_begin, nbr_off[hb] + cnt};
+          if (group_sampled(hb, ch * csz / SAMPLE_GROUP, P.sample))
+            units[w_unit++] = Unit{hb, ch, nbr_off[hb] + seg_begin, nbr_off[hb] + cnt};
       }
       ++nseg;
       seg_fill = 0;
@@ -446,7 +476,8 @@ __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __rest
   if (cnt > 0) {
     if (FILL) {
       for (uint32_t ch = 0; ch < nchunks; ++ch)
-        units[w_unit++] = Unit{hb, ch, nbr_off[hb] + seg_begin, nbr_off[hb] + cnt};
+        if (group_sampled(hb, ch * csz / SAMPLE_GROUP, P.sample))
+          units[w_unit++] = Unit{hb, ch, nbr_off[hb] + seg_begin, nbr_off[hb] + cnt};
     }
     ++nseg;
   }
@@ -454,7 +485,7 @@ __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __rest
     // a bin's unit count saturates at 2^32 - 1; the 64-bit totals of the
     // three count arrays (k_count_totals) then exceed the 32-bit offsets the
     // work lists use, and the call fails with MISTIC_ERR_TOO_LARGE
-    const unsigned long long nu = (unsigned long long)nseg * nchunks;
+    const unsigned long long nu = (unsigned long long)nseg * nchunks_s;
     const uint32_t nu32 = nu > 0xffffffffull ? 0xffffffffu : (uint32_t)nu;
     nbr_cnt[hb] = cnt;
     unit_cnt[hb] = tc ? 0u : nu32;

@@ -104,6 +104,7 @@ struct EnumParams {
   uint32_t chunk;    // home points per CUDA-core unit
   uint32_t tc_min;   // home bins with at least this many points get tensor-core units (0: none)
   uint32_t tc_chunk; // home points per tensor-core unit
+  uint32_t sample;   // > 1: only home points of sampled 512-point groups (mistic_opts.home_sample)
 };
 
 struct JoinParams {
@@ -143,11 +144,12 @@ struct TcParams {
   long long wait_limit;    // nanoseconds before a barrier wait gives up
   int stall_test;          // failure-detection test: the MMA warp never signals (waits run out)
   int prof;                // record per-role wait/total cycles into ctr->prof (diagnostics)
-  // long-row kernel (join_tcw.cu) only: split sorted rows and their norms
-  const void* xh;          // bf16 hi parts, n_rows x kd, row-major
-  const void* xl;          // bf16 lo parts, same layout
+  // long-row kernel (join_tcw.cu) only: prepared sorted rows and their norms
+  int prec;                // operand precision: 0 split bf16, 1 single bf16, 2 tf32
+  const void* xh;          // bf16 hi parts (prec 0, 1) or tf32-rounded FP32 rows (prec 2), n_rows x kd
+  const void* xl;          // bf16 lo parts (prec 0), same layout
   const float* xn;         // FP32 |x|^2 of the sorted rows
-  uint32_t kd;             // d rounded up to the K chunk
+  uint32_t kd;             // d rounded up to the stage's K
   uint64_t n_rows;         // rows of xh / xl
 };
 
@@ -246,11 +248,13 @@ bool tc_supported(uint32_t d);
 int tc_kp(uint32_t d);
 uint32_t tc_rows(uint32_t d);
 void run_tc(mistic_handle_s*, const JoinParams&, const TcParams&);
-// Long rows (tc_kp(d) > 128): K-chunked kernel over rows split once into
-// bf16 hi/lo (tcw_prepare: xh and xl hold n x tcw_kd(d) bf16 each, xn n floats).
-uint32_t tcw_kd(uint32_t d);
-void tcw_prepare(mistic_handle_s*, const float* xf, uint32_t dpad32, uint32_t d, size_t n, void* xh, void* xl,
-                 float* xn);
+// Long rows (tc_kp(d) > 128) and the tf32 mode: K-chunked kernel over rows
+// prepared once at operand precision `prec` (0: bf16 hi and lo in xh, xl;
+// 1: bf16 in xh; 2: tf32-rounded FP32 in xh; n x tcw_kd(d, prec) elements
+// each) with their FP32 norms in xn.
+uint32_t tcw_kd(uint32_t d, int prec);
+void tcw_prepare(mistic_handle_s*, int prec, const float* xf, uint32_t dpad32, uint32_t d, size_t n, void* xh,
+                 void* xl, float* xn);
 void run_tcw(mistic_handle_s*, const JoinParams&, const TcParams&);
 }  // namespace join
 

@@ -20,7 +20,8 @@
 // reference FP64 predicate value) gives T_lo = eps2/(1+g64) - E and
 // T_hi = eps2/(1-g64) + E: D <= T_lo accepts, D > T_hi rejects, anything in
 // between is re-decided with the reference FP64 predicate.  The bound covers
-//   - bf16 splitting: each product carries <= 3.02 * 2^-18 |A_k||B_k|,
+//   - bf16 splitting: each product carries <= 3.02 * 2^-16 |A_k||B_k| (bf16
+//     keeps 8 significant bits: |x - hi| <= 2^-8 |x|, |x - hi - lo| <= 2^-16 |x|),
 //   - tensor-core FP32 accumulation: taken as <= 2^-19 per MMA instruction
 //     relative to the sum of |products| (a generous allowance),
 //   - FP32 norms (g_d), the FP32 centring (2uR + u(|a'|+|q'|)),

@@ -25,13 +25,26 @@
 // columns.  A stage holds one K chunk of both home chunks and of the 256
 // candidate rows (64 KB); three stages are in flight.
 //
-// Exactness: the same rigorous bound as the short-row kernel (split error
-// 3.02 * 2^-18 per |a_k||q_k|, 2^-19 per MMA instruction of accumulation,
-// FP32 norms, global FP32 centring), plus the FP32 epilogue arithmetic
-// (accounted for in TcParams.kappa by the host): D' <= -dlt(n) accepts,
-// D' < 0 otherwise goes to the band list, whose pairs are re-decided with
-// the reference FP64 predicate.  Columns whose bound exceeds 0.1 eps2 are
-// re-decided entirely in FP64.
+// Operand precision (template PREC, chosen per call by the host):
+//   0  split bf16: G = Ahi.Bhi + Ahi.Blo + Alo.Bhi, 3 MMAs per K step of 16,
+//      stages of K = 32 as 64-byte rows (64B swizzle); operand error
+//      3.02 * 2^-16 of |a_k||q_k| (bf16 keeps 8 significant bits: the hi part
+//      is within 2^-8, hi + lo within 2^-16 of the value);
+//   1  single bf16: one MMA per K step of 16, stages of K = 64 as 128-byte
+//      rows (128B swizzle); a third of the tensor work, operand error
+//      2^-7 + 2^-16 -- used when the resulting band stays narrow (large eps
+//      relative to the rows' norms);
+//   2  tf32 (kind::tf32, rows rounded to tf32 once): one MMA per K step of 8,
+//      stages of K = 32 as 128-byte rows; operand error 2^-10 + 2^-22.
+// All three stage 64 KB a stage (home tiles 32 KB, candidates 32 KB).
+//
+// Exactness: the same rigorous bound as the short-row kernel (the operand
+// error above, 2^-19 per MMA instruction of accumulation, FP32 norms, global
+// FP32 centring), plus the FP32 epilogue arithmetic (accounted for in
+// TcParams.kappa by the host): D' <= -dlt(n) accepts, D' < 0 otherwise goes
+// to the band list, whose pairs are re-decided with the reference FP64
+// predicate.  Columns whose bound exceeds 0.1 eps2 are re-decided entirely
+// in FP64.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -54,7 +67,7 @@ using namespace tcu;
 constexpr int WM = 128;      // rows per home chunk (MMA M)
 constexpr int WG = 2;        // home chunks per unit
 constexpr int WN = 256;      // candidate columns per group (MMA N at most)
-constexpr int WKC = 32;      // K per pipeline stage (two MMA K steps of 16)
+constexpr int WKC = 32;      // K per pipeline stage of the split kernel (two MMA K steps of 16)
 constexpr int WNS = 3;       // stages
 constexpr int WWIN = 256;    // neighbour bins per candidate window
 constexpr int WNPW = 8;      // producer warps: thread t loads home row t and candidate row t
@@ -72,8 +85,17 @@ constexpr uint32_t B_HI = 2 * WG * A_CHUNK;     // 32 KB
 constexpr uint32_t B_LO = B_HI + WN * WKC * 2;  // 48 KB
 constexpr uint32_t STAGE_BYTES = B_LO + WN * WKC * 2;
 constexpr uint32_t SW_ATOM = 8 * WKC * 2;       // 8 rows x 64 B: the home rows' swizzle atom and MMA SBO
+// single-operand precisions (PREC 1, 2): 128-byte rows, home chunks 16 KB
+// each at 0, 16 KB, candidates at 32 KB
+constexpr uint32_t S_ACHUNK = WM * 128;         // 16 KB
+constexpr uint32_t S_B = WG * S_ACHUNK;         // 32 KB
+constexpr uint32_t SW_ATOM128 = 8 * 128;        // 8 rows x 128 B
 constexpr uint32_t WFLAG_END = 1;
 static_assert(WNPROD == WG * WM && WNPROD == WN, "one producer thread per operand row");
+static_assert(S_B + WN * 128 == STAGE_BYTES, "all precisions stage the same bytes");
+
+// K elements per stage, by precision
+__host__ __device__ constexpr uint32_t tcw_kstage(int prec) { return prec == 1 ? 64u : 32u; }
 
 // Everything the epilogue needs about one group (a unit's home rows x up to
 // 256 candidate columns).  Written by the producers before the group's first
@@ -122,6 +144,17 @@ __device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
   return d;
 }
 
+// The same for 128-byte rows, 128B swizzle: 8-row atoms of 1024 B (SBO).
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)((SW_ATOM128 >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version
+  d |= (uint64_t)2 << 61;  // layout: 128B swizzle
+  return d;
+}
+
 __device__ __forceinline__ void cp_async16_s(uint32_t dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
@@ -148,7 +181,8 @@ __device__ __forceinline__ void tma_tile_2d(uint32_t dst, uint64_t map, int x, i
 
 // One warp per sorted row: bf16 hi/lo split of the FP32 row (zero beyond its
 // dpad32 stored values, up to kd) into the row-major arrays xh, xl (kd bf16
-// a row), and its FP32 squared norm.
+// a row; xl null: the hi part alone, for the single-bf16 precision), and its
+// FP32 squared norm.
 __global__ void k_split_rows(const float* __restrict__ xf, uint32_t dpad32, uint32_t kd, size_t n,
                              uint4* __restrict__ xh, uint4* __restrict__ xl, float* __restrict__ xn) {
   const size_t row = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -181,7 +215,40 @@ __global__ void k_split_rows(const float* __restrict__ xf, uint32_t dpad32, uint
       pl[i] = *reinterpret_cast<const uint32_t*>(&lv);
     }
     oh_row[kb] = oh;
-    ol_row[kb] = ol;
+    if (xl) ol_row[kb] = ol;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(FULL_MASK, acc, o);
+  if (lane == 0) xn[row] = acc;
+}
+
+// One warp per sorted row: the FP32 row rounded to tf32 (round to nearest,
+// ties away; the low 13 bits are zero, so the tensor core reads it exactly),
+// zero beyond dpad32 up to kd, and its FP32 squared norm (of the unrounded
+// values).
+__global__ void k_tf32_rows(const float* __restrict__ xf, uint32_t dpad32, uint32_t kd, size_t n,
+                            float4* __restrict__ xt, float* __restrict__ xn) {
+  const size_t row = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float* x = xf + row * dpad32;
+  float4* o_row = xt + row * (kd / 4);
+  float acc = 0.f;
+  for (uint32_t c = lane; c < kd / 4; c += 32) {
+    float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (4 * c < dpad32) f = *reinterpret_cast<const float4*>(x + 4 * c);  // dpad32 % 4 == 0
+    acc = fmaf(f.x, f.x, acc);
+    acc = fmaf(f.y, f.y, acc);
+    acc = fmaf(f.z, f.z, acc);
+    acc = fmaf(f.w, f.w, acc);
+    float v[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      uint32_t t;
+      asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v[i]));
+      v[i] = __uint_as_float(t);
+    }
+    o_row[c] = make_float4(v[0], v[1], v[2], v[3]);
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(FULL_MASK, acc, o);
@@ -209,8 +276,11 @@ __global__ void k_split_rows(const float* __restrict__ xf, uint32_t dpad32, uint
 //   dfull[g]  MMA -> epilogue        (tcgen05.commit, or a plain arrive to stop)
 //   dfree[g]  epilogue -> MMA        (WNEPI arrivals; accumulator g reusable)
 //   gfree[x]  epilogue -> producers  (WNEPI arrivals; group slot x reusable)
+template <int PREC>
 __global__ void __launch_bounds__(WTHREADS, 1)
     k_join_tcw(const JoinParams P, const TcParams T, const __grid_constant__ TcwMaps M) {
+  constexpr uint32_t KST = tcw_kstage(PREC);     // K elements per stage
+  constexpr uint32_t ESZ = PREC == 2 ? 4u : 2u;  // operand element bytes
   extern __shared__ __align__(1024) unsigned char tcw_dyn[];
   __shared__ WShared S;
   // stages: WNS x STAGE_BYTES from the first 1024-byte boundary (swizzle atoms
@@ -219,7 +289,7 @@ __global__ void __launch_bounds__(WTHREADS, 1)
   const uint32_t stage_base = (dyn0 + 1023u) & ~1023u;
   unsigned long long* pstage = reinterpret_cast<unsigned long long*>(tcw_dyn + (stage_base - dyn0) + WNS * STAGE_BYTES);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t nkc = T.kd / WKC;   // stages per group
+  const uint32_t nkc = T.kd / KST;   // stages per group
   volatile uint32_t* abort_flag = &S.abort_flag;
 
   if (tid == 0) {
@@ -273,8 +343,12 @@ __global__ void __launch_bounds__(WTHREADS, 1)
     };
     const uint16_t* XH = static_cast<const uint16_t*>(T.xh);
     const uint16_t* XL = static_cast<const uint16_t*>(T.xl);
-    const uint32_t prow0 = 32u * (uint32_t)warp + ((uint32_t)lane >> 2);  // + 8 i
+    const unsigned char* XS = static_cast<const unsigned char*>(T.xh);  // single-operand rows (bf16 or tf32)
+    // split: lane l moves rows 32 w + l / 4 + 8 i (i < 4), piece l % 4;
+    // single: rows 32 w + l / 8 + 4 i (i < 8), 16-byte chunk l % 8
+    const uint32_t prow0 = 32u * (uint32_t)warp + ((uint32_t)lane >> (PREC == 0 ? 2 : 3));
     const uint32_t pkb = ((uint32_t)lane >> 1) & 1u, ph = (uint32_t)lane & 1u;
+    const uint32_t pch = (uint32_t)lane & 7u;
     for (;;) {
       const uint32_t slot = pf++ & 1;
       if (tid == 0) {
@@ -404,15 +478,21 @@ __global__ void __launch_bounds__(WTHREADS, 1)
         // rows by cp.async, lane l of warp w moving rows 32w + 8i + l / 4
         // (i = 0..3), piece l % 4 (K block 2j + (l % 4) / 2 of pair j, hi or
         // lo by l % 2): 8 rows x 32 bytes of hi and of lo per instruction
-        const uint16_t* b_src[4];
+        constexpr int NBR = PREC == 0 ? 4 : 8;  // candidate rows this thread moves
+        constexpr uint32_t RSTEP = PREC == 0 ? 8u : 4u;
+        const unsigned char* b_src[NBR];
         uint32_t b_ok = 0;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const uint32_t qi = __shfl_sync(FULL_MASK, q, 8 * i + (lane >> 2));  // column prow0 + 8 i
-          b_src[i] = (ph ? XL : XH) + (size_t)qi * T.kd;
-          if (prow0 + 8 * i < ncols) b_ok |= 1u << i;
+        for (int i = 0; i < NBR; ++i) {
+          // column prow0 + RSTEP i is owned by lane RSTEP i + lane / (32 / RSTEP) of this warp
+          const uint32_t qi = __shfl_sync(FULL_MASK, q, (int)(RSTEP * i) + (lane >> (PREC == 0 ? 2 : 3)));
+          if (PREC == 0)
+            b_src[i] = reinterpret_cast<const unsigned char*>((ph ? XL : XH) + (size_t)qi * T.kd);
+          else
+            b_src[i] = XS + ((size_t)qi * T.kd + 0) * ESZ + 16u * pch;
+          if (prow0 + RSTEP * i < ncols) b_ok |= 1u << i;
         }
-        const uint32_t abytes = ng * 2u * A_CHUNK;
+        const uint32_t abytes = ng * 2u * A_CHUNK;  // = ng x 16 KB at every precision
         for (uint32_t kc = 0; kc < nkc; ++kc) {
           const uint32_t s = step % WNS;
           const long long cs0 = T.prof ? clock64() : 0;
@@ -426,19 +506,34 @@ __global__ void __launch_bounds__(WTHREADS, 1)
             const uint32_t ab = smem_u32(&S.afull[s]);
             mbar_expect_tx(ab, abytes);
             for (uint32_t g = 0; g < ng; ++g) {
-              tma_tile_2d(sb + g * A_CHUNK, map_ah, (int)(kc * WKC), (int)(a0 + g * WM), ab);
-              tma_tile_2d(sb + A_LO + g * A_CHUNK, map_al, (int)(kc * WKC), (int)(a0 + g * WM), ab);
+              if (PREC == 0) {
+                tma_tile_2d(sb + g * A_CHUNK, map_ah, (int)(kc * WKC), (int)(a0 + g * WM), ab);
+                tma_tile_2d(sb + A_LO + g * A_CHUNK, map_al, (int)(kc * WKC), (int)(a0 + g * WM), ab);
+              } else {
+                tma_tile_2d(sb + g * S_ACHUNK, map_ah, (int)(kc * KST), (int)(a0 + g * WM), ab);
+              }
             }
           }
-          const uint32_t bdst = sb + (ph ? B_LO : B_HI);
+          if (PREC == 0) {
+            const uint32_t bdst = sb + (ph ? B_LO : B_HI);
 #pragma unroll
-          for (int j = 0; j < WKC / 16; ++j) {
-            const uint32_t kb = 2 * j + pkb;  // K block within the stage
+            for (int j = 0; j < WKC / 16; ++j) {
+              const uint32_t kb = 2 * j + pkb;  // K block within the stage
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-              const uint32_t r = prow0 + 8 * i;  // 64-byte row r, 16-byte chunk kb, 64B swizzle
-              const uint32_t off = r * 64u + ((kb ^ ((r >> 1) & 3u)) << 4);
-              if (b_ok & (1u << i)) cp_async16_s(bdst + off, b_src[i] + kc * WKC + kb * 8);
+              for (int i = 0; i < NBR; ++i) {
+                const uint32_t r = prow0 + 8 * i;  // 64-byte row r, 16-byte chunk kb, 64B swizzle
+                const uint32_t off = r * 64u + ((kb ^ ((r >> 1) & 3u)) << 4);
+                if (b_ok & (1u << i))
+                  cp_async16_s(bdst + off, b_src[i] + (size_t)(kc * WKC + kb * 8) * 2);
+              }
+            }
+          } else {
+            // 128-byte rows: 16-byte chunk pch of row r at r * 128 + 16 (pch ^ (r & 7))
+#pragma unroll
+            for (int i = 0; i < NBR; ++i) {
+              const uint32_t r = prow0 + RSTEP * i;
+              const uint32_t off = r * 128u + ((pch ^ (r & 7u)) << 4);
+              if (b_ok & (1u << i)) cp_async16_s(sb + S_B + off, b_src[i] + (size_t)kc * KST * ESZ);
             }
           }
           // this thread's arrival on the stage's full barrier is made by the
@@ -521,7 +616,7 @@ __global__ void __launch_bounds__(WTHREADS, 1)
         }
         const uint32_t ng = Gm.ng;
         const uint32_t nmma = max(16u, (Gm.ncols + 15u) & ~15u);  // MMA N: the group's columns, rounded to 16
-        const uint32_t idesc = umma_idesc(WM, (int)nmma);
+        const uint32_t idesc = umma_idesc_fmt(WM, (int)nmma, PREC == 2 ? 2u : 1u);
         for (uint32_t kc = 0; kc < nkc && ok; ++kc) {
           if (kc > 0) {
             s = step % WNS;
@@ -546,18 +641,32 @@ __global__ void __launch_bounds__(WTHREADS, 1)
               if (!ok) break;
               asm volatile("tcgen05.fence::after_thread_sync;");
             }
-            const uint32_t ah = sb + g * A_CHUNK, al = sb + A_LO + g * A_CHUNK;
             const uint32_t dt = tbase + g * WN;
+            if (PREC == 0) {
+              const uint32_t ah = sb + g * A_CHUNK, al = sb + A_LO + g * A_CHUNK;
 #pragma unroll
-            for (int ks = 0; ks < WKC / 16; ++ks) {
-              // K step of 16 bf16: 32 bytes into the 64-byte swizzled rows of
-              // both operands
-              const uint32_t ok16 = ks * 32;
-              const uint64_t dah = desc_sw64(ah + ok16), dal = desc_sw64(al + ok16);
-              const uint64_t dbh = desc_sw64(bh + ok16), dbl = desc_sw64(bl + ok16);
-              mma_bf16(dt, dah, dbh, idesc, (kc | ks) ? 1u : 0u);
-              mma_bf16(dt, dah, dbl, idesc, 1u);
-              mma_bf16(dt, dal, dbh, idesc, 1u);
+              for (int ks = 0; ks < WKC / 16; ++ks) {
+                // K step of 16 bf16: 32 bytes into the 64-byte swizzled rows of
+                // both operands
+                const uint32_t ok16 = ks * 32;
+                const uint64_t dah = desc_sw64(ah + ok16), dal = desc_sw64(al + ok16);
+                const uint64_t dbh = desc_sw64(bh + ok16), dbl = desc_sw64(bl + ok16);
+                mma_bf16(dt, dah, dbh, idesc, (kc | ks) ? 1u : 0u);
+                mma_bf16(dt, dah, dbl, idesc, 1u);
+                mma_bf16(dt, dal, dbh, idesc, 1u);
+              }
+            } else {
+              const uint32_t a1 = sb + g * S_ACHUNK, b1 = sb + S_B;
+#pragma unroll
+              for (int ks = 0; ks < 4; ++ks) {
+                // one K step (16 bf16 or 8 tf32) = 32 bytes into the 128-byte
+                // swizzled rows of both operands
+                const uint64_t da = desc_sw128(a1 + ks * 32), db = desc_sw128(b1 + ks * 32);
+                if (PREC == 2)
+                  mma_tf32(dt, da, db, idesc, (kc | ks) ? 1u : 0u);
+                else
+                  mma_bf16(dt, da, db, idesc, (kc | ks) ? 1u : 0u);
+              }
             }
           }
           if (!ok) break;
@@ -710,15 +819,24 @@ __global__ void __launch_bounds__(WTHREADS, 1)
 
 namespace join {
 
-uint32_t tcw_kd(uint32_t d) { return (d + WKC - 1) / WKC * WKC; }
+uint32_t tcw_kd(uint32_t d, int prec) {
+  const uint32_t ks = tcw_kstage(prec);
+  return (d + ks - 1) / ks * ks;
+}
 
-void tcw_prepare(mistic_handle_s* h, const float* xf, uint32_t dpad32, uint32_t d, size_t n, void* xh, void* xl,
-                 float* xn) {
+void tcw_prepare(mistic_handle_s* h, int prec, const float* xf, uint32_t dpad32, uint32_t d, size_t n, void* xh,
+                 void* xl, float* xn) {
   if (n == 0) return;
   const unsigned rows_per_block = 8;
   const unsigned grid = (unsigned)((n + rows_per_block - 1) / rows_per_block);
-  k_split_rows<<<grid, rows_per_block * 32, 0, h->stream>>>(xf, dpad32, tcw_kd(d), n, (uint4*)xh, (uint4*)xl, xn);
-  launched(h, "split_rows");
+  if (prec == 2) {
+    k_tf32_rows<<<grid, rows_per_block * 32, 0, h->stream>>>(xf, dpad32, tcw_kd(d, prec), n, (float4*)xh, xn);
+    launched(h, "tf32_rows");
+  } else {
+    k_split_rows<<<grid, rows_per_block * 32, 0, h->stream>>>(xf, dpad32, tcw_kd(d, prec), n, (uint4*)xh,
+                                                              prec == 0 ? (uint4*)xl : nullptr, xn);
+    launched(h, "split_rows");
+  }
 }
 
 namespace {
@@ -736,38 +854,55 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// bf16 rows of kd elements (row pitch kd * 2 bytes), n rows; box: 32 x rows.
-void encode_rows(CUtensorMap* m, const void* base, uint32_t kd, size_t n, uint32_t box_rows) {
+// Operand rows of kd elements, n rows; box: one stage's K x box_rows.  Split
+// precision: bf16, 64-byte box rows, 64B swizzle; single bf16 or tf32:
+// 128-byte box rows, 128B swizzle.
+void encode_rows(CUtensorMap* m, const void* base, int prec, uint32_t kd, size_t n, uint32_t box_rows) {
+  const uint32_t esz = prec == 2 ? 4 : 2;
   const cuuint64_t dims[2] = {kd, (cuuint64_t)n};
-  const cuuint64_t strides[1] = {(cuuint64_t)kd * 2};
-  const cuuint32_t box[2] = {(cuuint32_t)WKC, box_rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)kd * esz};
+  const cuuint32_t box[2] = {tcw_kstage(prec), box_rows};
   const cuuint32_t estr[2] = {1, 1};
-  const CUresult r = encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
-                                 estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+  const CUresult r = encode_fn()(m, prec == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                                 const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                 prec == 0 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) throw Error(MISTIC_ERR_CUDA, "cuTensorMapEncodeTiled failed for the split rows");
+  if (r != CUDA_SUCCESS) throw Error(MISTIC_ERR_CUDA, "cuTensorMapEncodeTiled failed for the operand rows");
+}
+
+template <int PREC>
+void launch_tcw(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
+  TcwMaps maps;
+  encode_rows(&maps.ah, T.xh, PREC, T.kd, T.n_rows, WM);
+  if (PREC == 0)
+    encode_rows(&maps.al, T.xl, PREC, T.kd, T.n_rows, WM);
+  else
+    maps.al = maps.ah;  // unused
+  const size_t dyn = 1024 + (size_t)WNS * STAGE_BYTES + (size_t)2 * WNEPI * PSTAGE * sizeof(unsigned long long);
+  MCK(cudaFuncSetAttribute(k_join_tcw<PREC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  MCK(cudaFuncSetAttribute(k_join_tcw<PREC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  int per_sm = 0;
+  MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join_tcw<PREC>, WTHREADS, dyn));
+  if (per_sm < 1) throw Error(MISTIC_ERR_TOO_LARGE, "long-row tensor-core join does not fit on an SM");
+  const unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)h->sms, T.n_units);
+  if (getenv("MISTIC_DEBUG"))
+    fprintf(stderr, "[mistic] join_tcw PREC=%d KD=%u dyn=%zu occupancy=%d grid=%u units=%llu\n", PREC, T.kd, dyn,
+            per_sm, grid, (unsigned long long)T.n_units);
+  k_join_tcw<PREC><<<grid, WTHREADS, dyn, h->stream>>>(P, T, maps);
+  launched(h, "join_tcw");
 }
 }  // namespace
 
 void run_tcw(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
   if (T.n_units == 0) return;
-  if (!T.xh || !T.xl || !T.xn || T.kd % WKC || T.n_rows == 0)
-    throw Error(MISTIC_ERR_INTERNAL, "long-row tensor-core join without split rows");
-  TcwMaps maps;
-  encode_rows(&maps.ah, T.xh, T.kd, T.n_rows, WM);
-  encode_rows(&maps.al, T.xl, T.kd, T.n_rows, WM);
-  const size_t dyn = 1024 + (size_t)WNS * STAGE_BYTES + (size_t)2 * WNEPI * PSTAGE * sizeof(unsigned long long);
-  MCK(cudaFuncSetAttribute(k_join_tcw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-  MCK(cudaFuncSetAttribute(k_join_tcw, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-  int per_sm = 0;
-  MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join_tcw, WTHREADS, dyn));
-  if (per_sm < 1) throw Error(MISTIC_ERR_TOO_LARGE, "long-row tensor-core join does not fit on an SM");
-  const unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)h->sms, T.n_units);
-  if (getenv("MISTIC_DEBUG"))
-    fprintf(stderr, "[mistic] join_tcw KD=%u dyn=%zu occupancy=%d grid=%u units=%llu\n", T.kd, dyn, per_sm, grid,
-            (unsigned long long)T.n_units);
-  k_join_tcw<<<grid, WTHREADS, dyn, h->stream>>>(P, T, maps);
-  launched(h, "join_tcw");
+  if (T.prec < 0 || T.prec > 2 || !T.xh || (T.prec == 0 && !T.xl) || !T.xn || T.kd == 0 ||
+      T.kd % tcw_kstage(T.prec) || T.n_rows == 0)
+    throw Error(MISTIC_ERR_INTERNAL, "long-row tensor-core join without prepared operand rows");
+  switch (T.prec) {
+    case 0: launch_tcw<0>(h, P, T); break;
+    case 1: launch_tcw<1>(h, P, T); break;
+    default: launch_tcw<2>(h, P, T); break;
+  }
 }
 
 }  // namespace join

@@ -317,14 +317,55 @@ int bit_length(uint64_t v) {
 //   5M x 18:    T = 48: 150.2, 61: 147.0, 80: 145.2, 100: 145.1, 128: 146.8
 //   515k x 90:  T = 1: 259.9, 2: 261.9, 4: 261.9, 8: 263.3
 // hence 29000 / d^2, clamped to [1, 96].
-uint32_t tc_min_bin(uint32_t d) {
+uint32_t tc_min_bin(uint32_t d, bool wide) {
   const char* e = getenv("MISTIC_TC_MIN_BIN");
   if (e && *e) return (uint32_t)std::max(1l, strtol(e, nullptr, 10));
   // long rows (K-chunked kernel): a tile costs ~3 * 2 * 128 * d tensor flops
   // per candidate column whatever its home rows, the FP32 CUDA cores 3 d per
   // row and column; measured on 2M x 384: T = 8: 1383, 16: 1422, 24: 1514 ms
-  if (join::tc_kp(d) > 128) return 8;
+  if (wide) return 8;
   return (uint32_t)std::min(96.0, std::max(1.0, std::floor(29000.0 / ((double)d * d))));
+}
+
+// Relative error allowance per (|a'| + |q'|)^2 + 1.2 eps2 of a tensor-core
+// join (TcParams.kappa): operand rounding per |a_k||q_k| + FP32
+// accumulation (2^-19 per MMA instruction along K; measured worst case on
+// GB300 below 0.09 of that) + FP32 norms + ...  Operand rounding: bf16 keeps
+// 8 significant bits (unit roundoff 2^-8) and tf32 11 (2^-11), so with
+// x = hi + lo + r, |x - hi| <= 2^-8 |x|, |r| <= 2^-16 |x|:
+//   split bf16 (hi.hi + hi.lo + lo.hi)  3.02 * 2^-16,
+//   single bf16                         2 * 2^-8 + 2^-16 = 2^-7 + 2^-16,
+//   tf32 (rounded to nearest)           2 * 2^-11 + 2^-22 = 2^-10 + 2^-22,
+// and then
+// FP32 norms + the rounding of the folded column |q'|^2 - T (short rows), or
+// of the three FP32 operations forming D' = |a|^2 - 2G + (|q|^2 - T) in the
+// long-row kernel's epilogue (each within u (|a| + |q|)^2 + u T).
+double tc_kappa(uint32_t d, bool wide, int prec) {
+  const double u = ldexp(1.0, -24) * (1.0 + ldexp(1.0, -20));
+  const double gd = d * u / (1.0 - d * u);
+  const double op = prec == 1 ? ldexp(1.0, -7) + ldexp(1.0, -16)
+                              : (prec == 2 ? ldexp(1.0, -10) + ldexp(1.0, -22) : 3.02 * ldexp(1.0, -16));
+  const int n_mma = wide ? (prec == 0 ? 3 : 1) * (int)join::tcw_kd(d, prec) / (prec == 2 ? 8 : 16)
+                         : 3 * join::tc_kp(d) / 16;
+  return ((op + n_mma * 1.01 * ldexp(1.0, -19)) * (1.0 + gd) + gd + (wide ? 5.0 : 1.0) * u) * 1.01;
+}
+
+// Operand precision of the K-chunked tensor-core join.  TF32 mode: tf32.
+// Otherwise single bf16 (a third of the split's tensor work) when even the
+// widest column's bound -- rows at the largest norm R from the centre --
+// stays within the cap of eps^2 / 10 (no column is left wholly to FP64);
+// else split bf16.  MISTIC_TC_PREC=split|bf16 overrides (tuning).
+int tc_precision(mistic_mode mode, uint32_t d, double eps2, double R) {
+  if (mode == MISTIC_MODE_TF32) return 2;
+  if (const char* e = getenv("MISTIC_TC_PREC")) {
+    if (!strcmp(e, "split")) return 0;
+    if (!strcmp(e, "bf16")) return 1;
+  }
+  const double u = ldexp(1.0, -24);
+  const double rs = 2.0 * R, Dp = 1.1 * sqrt(eps2);
+  const double delta = 2.0 * u * R + u * rs;
+  const double E = tc_kappa(d, true, 1) * (rs * rs + 1.2 * eps2) + delta * (2.0 * Dp + delta);
+  return E <= 0.1 * eps2 ? 1 : 0;
 }
 
 void check_handle(mistic_handle h) {
@@ -355,7 +396,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   if (n >= 0xffffffffull) throw Error(MISTIC_ERR_TOO_LARGE, "n must be below 2^32 - 1");
   if (n > 0 && !pts) throw Error(MISTIC_ERR_INVALID_ARG, "null points");
   if (o.mode != MISTIC_MODE_AUTO && o.mode != MISTIC_MODE_FP64 && o.mode != MISTIC_MODE_FP32 &&
-      o.mode != MISTIC_MODE_BF16)
+      o.mode != MISTIC_MODE_BF16 && o.mode != MISTIC_MODE_TF32)
     throw Error(MISTIC_ERR_INVALID_ARG, "unknown mode");
   if (o.pairs != MISTIC_PAIRS_NONE && o.pairs != MISTIC_PAIRS_HOST && o.pairs != MISTIC_PAIRS_DEVICE)
     throw Error(MISTIC_ERR_INVALID_ARG, "unknown pairs destination");
@@ -564,17 +605,25 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   // augmented K fits one operand tile
   // AUTO takes the tensor cores from d = 8 up (measured faster than the FP32
   // filter on the 5M x 18 join); below that the augmented K is mostly padding
+  const bool tf32_mode = o.mode == MISTIC_MODE_TF32;
   const bool use_tc = !fp64 && join::tc_supported(d) && eps2 > 1e-20 &&
-                      (o.mode == MISTIC_MODE_BF16 || (o.mode == MISTIC_MODE_AUTO && d >= 8));
-  r->mode_used = fp64 ? MISTIC_MODE_FP64 : (use_tc ? MISTIC_MODE_BF16 : MISTIC_MODE_FP32);
+                      (o.mode == MISTIC_MODE_BF16 || tf32_mode || (o.mode == MISTIC_MODE_AUTO && d >= 8));
+  // long rows (augmented K above one 128-wide operand tile), and every row in
+  // tf32 mode, use the K-chunked kernel over rows prepared once; its operand
+  // precision is picked from the bound (see tc_precision)
+  const bool wide = use_tc && (tf32_mode || join::tc_kp(d) > 128);
+  const int prec = wide ? tc_precision(o.mode, d, eps2, R) : 0;
+  r->mode_used = fp64 ? MISTIC_MODE_FP64
+                      : (use_tc ? (tf32_mode ? MISTIC_MODE_TF32 : MISTIC_MODE_BF16) : MISTIC_MODE_FP32);
   clk.mark();  // 5
 
   // ---- neighbour enumeration -> work units
   const int CH = join::chunk_for(fp64, fp64 ? dpad64 : dpad32);
   ep.chunk = (uint32_t)CH;
   ep.seg_cap = 4096;
-  ep.tc_min = use_tc ? tc_min_bin(d) : 0u;
-  ep.tc_chunk = use_tc ? join::tc_rows(d) : 128;
+  ep.sample = o.home_sample;
+  ep.tc_min = use_tc ? tc_min_bin(d, wide) : 0u;
+  ep.tc_chunk = use_tc ? (wide ? 256u : join::tc_rows(d)) : 128;
   uint32_t* nbr_cnt = abuf<uint32_t>(h, "nbr_cnt", m + 1);
   uint32_t* unit_cnt = abuf<uint32_t>(h, "unit_cnt", m + 1);
   uint32_t* unit_cnt_tc = abuf<uint32_t>(h, "unit_cnt_tc", m + 1);
@@ -638,10 +687,6 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     const double u = ldexp(1.0, -24) * (1.0 + ldexp(1.0, -20));
     const double gd = d * u / (1.0 - d * u);
     const double g64 = (d + 2) * ldexp(1.0, -53) * 1.01;
-    // long rows (augmented K above one 128-wide operand tile) use the
-    // K-chunked kernel over rows split once into bf16 hi/lo
-    const bool wide = join::tc_kp(d) > 128;
-    const int n_mma = 3 * (wide ? (int)join::tcw_kd(d) : join::tc_kp(d)) / 16;
     tp.units = units_tc;
     tp.n_units = tots[2];
     tp.ctr = ctr + 1;
@@ -649,12 +694,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     if ((double)tp.eps2_lo > eps2 / (1.0 + g64)) tp.eps2_lo = nextafterf(tp.eps2_lo, 0.f);
     tp.eps2_hi = (float)(eps2 / (1.0 - g64));
     if ((double)tp.eps2_hi < eps2 / (1.0 - g64)) tp.eps2_hi = nextafterf(tp.eps2_hi, INFINITY);
-    // split error + MMA accumulation (2^-19 per instruction) + FP32 norms +
-    // rounding of the folded column |q'|^2 - T, per (|a'| + |q'|)^2 + 1.2 eps2
-    // (the long-row kernel forms D' = |a|^2 - 2G + (|q|^2 - T) in FP32: three
-    // roundings, each within u (|a| + |q|)^2 + u T, instead of the folded column)
-    tp.kappa = (float)(((3.02 * ldexp(1.0, -18) + n_mma * 1.01 * ldexp(1.0, -19)) * (1.0 + gd) + gd +
-                        (wide ? 5.0 : 1.0) * u) * 1.01);
+    tp.kappa = (float)tc_kappa(d, wide, prec);
     tp.ginf = (float)(1.0 / (1.0 - gd) * (1.0 + 1e-6));
     tp.uR2 = (float)(2.0 * u * R * 1.0001);
     tp.u1 = (float)(u * (1.0 + u) * 1.0001);
@@ -668,12 +708,14 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     tp.stall_test = (st && *st == '1') ? 1 : 0;
     tp.wait_limit = tp.stall_test ? 2000000ll : 2000000000ll;  // 2 ms in the test, else 2 s
     tp.prof = getenv("MISTIC_DEBUG") ? 1 : 0;
+    tp.prec = prec;
     if (wide && tots[2] > 0) {
-      tp.kd = join::tcw_kd(d);
-      uint16_t* xh = abuf<uint16_t>(h, "xh", n * (size_t)tp.kd);
-      uint16_t* xl = abuf<uint16_t>(h, "xl", n * (size_t)tp.kd);
+      tp.kd = join::tcw_kd(d, prec);
+      // operand rows: bf16 (hi, and lo for the split) or tf32 in FP32 words
+      void* xh = h->arena.get("xh", n * (size_t)tp.kd * (prec == 2 ? 4 : 2));
+      void* xl = prec == 0 ? h->arena.get("xl", n * (size_t)tp.kd * 2) : nullptr;
       float* xn = abuf<float>(h, "xn", n);
-      join::tcw_prepare(h, xf, dpad32, d, n, xh, xl, xn);
+      join::tcw_prepare(h, prec, xf, dpad32, d, n, xh, xl, xn);
       tp.xh = xh;
       tp.xl = xl;
       tp.xn = xn;
@@ -723,7 +765,12 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     if (o.timing) MCK(cudaEventRecord(h->jev[0], h->stream));
     join::run(h, fp64, CH, jp);
     if (o.timing) MCK(cudaEventRecord(h->jev[1], h->stream));
-    if (use_tc) join::run_tc(h, jp, tp);
+    if (use_tc) {
+      if (wide)
+        join::run_tcw(h, jp, tp);
+      else
+        join::run_tc(h, jp, tp);
+    }
     if (o.timing) MCK(cudaEventRecord(h->jev[2], h->stream));
     join::run_band(h, jp);
     d2h(h, &hc, ctr, sizeof hc);
@@ -751,6 +798,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   r->pairs_ordered_incl_self = 2 * hc.pairs + n;
   r->band_pairs = fp64 ? 0 : hc.band;
   r->ulp_ambiguous = hc.ambiguous;
+  r->tc_operands = (use_tc && tots[2] > 0) ? (wide ? 1 + prec : 1) : 0;
   if (use_tc) {
     JoinCounters tcc{};
     d2h(h, &tcc, ctr + 1, sizeof tcc);

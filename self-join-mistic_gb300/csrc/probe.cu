@@ -42,13 +42,6 @@ __device__ __forceinline__ uint32_t core_off(uint32_t r, uint32_t c, uint32_t ro
   return ((r >> 3) * (row_bytes / 16) + c) * 128 + (r & 7) * 16;
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-      "l"(da), "l"(db), "r"(idesc), "r"(acc));
-}
-
 __global__ void __launch_bounds__(128, 1)
     k_tc_probe(const unsigned char* __restrict__ a, const unsigned char* __restrict__ b, uint32_t row_bytes, int kind,
                uint32_t n_inst, float* __restrict__ d, uint32_t* __restrict__ status) {
@@ -82,9 +75,7 @@ __global__ void __launch_bounds__(128, 1)
   const uint32_t tbase = S.tmem_base;
   if (tid == 0) {
     const uint32_t sbo = 8 * row_bytes;
-    const uint32_t fmt = kind == 1 ? 2u : 1u;  // TF32 : BF16
-    const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(PN >> 3) << 17) |
-                           ((uint32_t)(PM >> 4) << 24);
+    const uint32_t idesc = umma_idesc_fmt(PM, PN, kind == 1 ? 2u : 1u);  // TF32 : BF16
     const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
     for (uint32_t ks = 0; ks < n_inst; ++ks) {
       const uint32_t o = ks * 256;  // 32 bytes of K per instruction = two core matrices

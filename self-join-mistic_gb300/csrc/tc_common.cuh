@@ -28,15 +28,27 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t sbo) {
   return d;
 }
 
-// Instruction descriptor, kind::f16: D f32, A/B bf16, both K-major, N x M.
-__host__ __device__ constexpr uint32_t umma_idesc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor: D f32, A/B of format `fmt` (1: bf16 under
+// kind::f16, 2: tf32 under kind::tf32), both K-major, N x M.
+__host__ __device__ constexpr uint32_t umma_idesc_fmt(int M, int N, uint32_t fmt) {
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
+// kind::f16 with bf16 operands
+__host__ __device__ constexpr uint32_t umma_idesc(int M, int N) { return umma_idesc_fmt(M, N, 1u); }
 
 __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+      "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+// kind::tf32: FP32 operands of which the tensor core reads the top 19 bits
+// (the joins round them to tf32 beforehand, so nothing is dropped here)
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
       "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 

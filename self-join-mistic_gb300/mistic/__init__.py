@@ -19,7 +19,8 @@ from . import _lib as L
 
 __all__ = ["MisticError", "JoinResult", "Handle", "selfjoin", "read_points", "convert_text"]
 
-MODES = {"auto": L.MODE_AUTO, "fp64": L.MODE_FP64, "fp32": L.MODE_FP32, "bf16": L.MODE_BF16}
+MODES = {"auto": L.MODE_AUTO, "fp64": L.MODE_FP64, "fp32": L.MODE_FP32, "bf16": L.MODE_BF16,
+         "tf32": L.MODE_TF32}
 RP_MODES = {"pca": L.RP_PCA, "box": L.RP_BOX, "user": L.RP_USER}
 
 
@@ -52,6 +53,7 @@ class JoinResult:
     csr_offsets: np.ndarray | None = None    # (n + 1,) uint64, host CSR table
     csr_nbrs: np.ndarray | None = None       # (offsets[n],) uint32
     device_pairs: int | None = None          # device pointer when pairs="device"
+    tc_operands: str = "none"                # tensor-core operands: none, split-bf16, bf16, tf32
     extra: dict = field(default_factory=dict)
 
 
@@ -91,7 +93,7 @@ class Handle:
 
     def opts(self, mode="auto", rp="pca", seed=0, pairs="none", sort_pairs=False,
              pair_capacity=0, input_on_device=False, check_finite=True, timing=True,
-             rp_user=None, pair_buffer=None, csr="none") -> L.Opts:
+             rp_user=None, pair_buffer=None, csr="none", home_sample=0) -> L.Opts:
         o = L.Opts()
         self.lib.mistic_opts_init(ctypes.byref(o))
         o.mode = MODES[mode]
@@ -106,6 +108,7 @@ class Handle:
         o.check_finite = 1 if check_finite else 0
         o.timing = 1 if timing else 0
         o.csr = {"none": L.PAIRS_NONE, "host": L.PAIRS_HOST, "device": L.PAIRS_DEVICE}[csr]
+        o.home_sample = home_sample
         if rp_user is not None:
             self._rp_keep = np.ascontiguousarray(rp_user, dtype=np.float64)
             o.rp_user = self._rp_keep.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
@@ -147,9 +150,10 @@ class Handle:
             band_pairs=r.band_pairs, ulp_ambiguous=r.ulp_ambiguous, n_bins=r.n_bins,
             n_bin_pairs=r.n_bin_pairs, n_units=r.n_units, n_units_tc=r.n_units_tc,
             tc_tiles=r.tc_tiles, tc_cells=r.tc_cells,
-            mode_used={0: "auto", 1: "fp64", 2: "fp32", 3: "bf16"}.get(r.mode_used, "?"),
+            mode_used={0: "auto", 1: "fp64", 2: "fp32", 3: "bf16", 4: "tf32"}.get(r.mode_used, "?"),
             ms=ms, kernel_launches=r.kernel_launches, pairs=pairs, device_pairs=dev,
-            csr_offsets=csr_off, csr_nbrs=csr_nb)
+            csr_offsets=csr_off, csr_nbrs=csr_nb,
+            tc_operands={0: "none", 1: "split-bf16", 2: "bf16", 3: "tf32"}.get(r.tc_operands, "?"))
         if not keep_device or not r.pairs_on_device:
             self.lib.mistic_result_free(ctypes.byref(r))
         else:

@@ -20,7 +20,7 @@ ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_TOO_LARGE = 1, 2, 3, 4
 ERR_NOT_FINITE, ERR_PAIR_OVERFLOW, ERR_TIMEOUT, ERR_NO_DEVICE = 5, 6, 7, 8
 ERR_IO, ERR_INTERNAL = 9, 10
 F64, F32 = 0, 1
-MODE_AUTO, MODE_FP64, MODE_FP32, MODE_BF16 = 0, 1, 2, 3
+MODE_AUTO, MODE_FP64, MODE_FP32, MODE_BF16, MODE_TF32 = 0, 1, 2, 3, 4
 RP_PCA, RP_BOX, RP_USER = 0, 1, 2
 PAIRS_NONE, PAIRS_HOST, PAIRS_DEVICE = 0, 1, 2
 
@@ -53,6 +53,7 @@ class Opts(ctypes.Structure):
         ("check_finite", i32),
         ("timing", i32),
         ("csr", i32),
+        ("home_sample", u32),
     ]
 
 
@@ -84,6 +85,7 @@ class Result(ctypes.Structure):
         ("csr_offsets", ctypes.POINTER(u64)),
         ("csr_nbrs", ctypes.POINTER(u32)),
         ("csr_on_device", i32),
+        ("tc_operands", i32),
         ("_owner", vp),
     ]
 

@@ -12,8 +12,10 @@ seeded stand-ins with the same shapes and comparable value distributions:
                 basis, spectrum i^-1.2), column-standardised; k=8, 16 nbrs
   batch2000     2,000 independent instances, n log-uniform in [1e3, 2e5],
                 d in {2,8,18,32,57,90}, FP32 anisotropic Gaussian mixtures
-  tiny384       n=5,000,000 d=384 FP32, 1,000 Zipf(1.1)-sized anisotropic
-                Gaussian clusters, L2-normalised; k=8, 16 nbrs
+  tiny384       n=5,000,000 d=384 FP32, 1,000 Zipf(1.1)-sized Gaussian
+                clusters, each with a full-rank covariance R diag(eig) R^T
+                (R a random rotation, the 384 eigenvalues log-uniform in
+                [1e-3, 1]), L2-normalised; k=8, 16 nbrs
 
 ε is calibrated by bisection on a seeded 10,000-point sample: the mean
 neighbour count of the full set is estimated as (n-1)/(|S|-1) times the mean
@@ -104,9 +106,13 @@ def gen_msd_like(n: int = 515_345, d: int = 90, seed: int = 3) -> np.ndarray:
 def gen_clusters(n: int, d: int, n_clusters: int, seed: int,
                  zipf: float | None = None, normalise: bool = False,
                  eig_lo: float = 1e-3, eig_hi: float = 1.0,
-                 dtype=np.float32) -> np.ndarray:
-    """Gaussian mixture with per-cluster random rotation and log-uniform
-    eigenvalues; cluster sizes Zipf(zipf) when given, else multinomial."""
+                 dtype=np.float32, rank: int | None = None) -> np.ndarray:
+    """Gaussian mixture: cluster c has covariance R_c diag(eig_c) R_c^T with
+    R_c a random rotation (QR of a Gaussian matrix) and eig_c log-uniform in
+    [eig_lo, eig_hi].  rank=None: full rank (all d eigenvalues); rank=r: the
+    rotation spans a random min(d, r)-dimensional subspace and every point
+    gets isotropic noise of variance eig_lo on top.  Cluster sizes Zipf(zipf) when given, else
+    multinomial with random weights."""
     rng = np.random.default_rng(seed)
     if zipf is not None:
         w = 1.0 / np.arange(1, n_clusters + 1, dtype=np.float64) ** zipf
@@ -117,20 +123,17 @@ def gen_clusters(n: int, d: int, n_clusters: int, seed: int,
     out = np.empty((n, d), dtype=dtype)
     pos = 0
     centres = rng.normal(size=(n_clusters, d))
+    r = d if rank is None else min(d, rank)
     for c in range(n_clusters):
         m = int(sizes[c])
         if m == 0:
             continue
-        # random rotation restricted to a low-rank frame keeps this cheap for
-        # d = 384: the covariance is R diag(eig) R^T with R a random
-        # orthogonal basis of a min(d, 32)-dimensional subspace plus isotropic
-        # floor eig_lo on the complement.
-        r = min(d, 32)
         basis, _ = np.linalg.qr(rng.normal(size=(d, r)))
         eig = np.exp(rng.uniform(math.log(eig_lo), math.log(eig_hi), size=r))
         z = rng.normal(size=(m, r)) * np.sqrt(eig)
         pts = centres[c] * 0.5 + z @ basis.T
-        pts += rng.normal(scale=math.sqrt(eig_lo), size=(m, d))
+        if rank is not None:
+            pts += rng.normal(scale=math.sqrt(eig_lo), size=(m, d))
         out[pos:pos + m] = pts
         pos += m
     perm = rng.permutation(n)
@@ -145,8 +148,8 @@ def gen_clusters(n: int, d: int, n_clusters: int, seed: int,
 
 def gen_clusters_device(n: int, d: int, n_clusters: int, seed: int, zipf: float = 1.1,
                         eig_lo: float = 1e-3, eig_hi: float = 1.0, device: str = "cuda"):
-    """The generator of gen_clusters (Zipf cluster sizes, low-rank random
-    rotation x log-uniform eigenvalues plus an isotropic floor, rows
+    """The generator of gen_clusters at full rank (Zipf cluster sizes, a
+    random rotation times d log-uniform eigenvalues per cluster, rows
     L2-normalised), drawn with a seeded torch generator on the GPU so that a
     5M x 384 set takes seconds instead of many minutes.  Returns an FP32
     host array.  The values differ from gen_clusters (another random
@@ -158,20 +161,19 @@ def gen_clusters_device(n: int, d: int, n_clusters: int, seed: int, zipf: float 
     sizes = np.random.default_rng(seed).multinomial(n, (w / w.sum()).numpy())
     out = torch.empty((n, d), dtype=torch.float32, device=device)
     centres = torch.randn((n_clusters, d), generator=g, device=device, dtype=torch.float32)
-    r = min(d, 32)
     pos = 0
-    for c in range(n_clusters):
-        m = int(sizes[c])
-        if m == 0:
-            continue
-        basis, _ = torch.linalg.qr(torch.randn((d, r), generator=g, device=device, dtype=torch.float32))
-        u = torch.rand((r,), generator=g, device=device, dtype=torch.float32)
+    for c0 in range(0, n_clusters, 50):  # rotations 50 at a time (batched QR)
+        c1 = min(n_clusters, c0 + 50)
+        basis, _ = torch.linalg.qr(torch.randn((c1 - c0, d, d), generator=g, device=device, dtype=torch.float32))
+        u = torch.rand((c1 - c0, d), generator=g, device=device, dtype=torch.float32)
         eig = torch.exp(math.log(eig_lo) + u * (math.log(eig_hi) - math.log(eig_lo)))
-        z = torch.randn((m, r), generator=g, device=device, dtype=torch.float32) * eig.sqrt()
-        blk = centres[c] * 0.5 + z @ basis.T
-        blk += torch.randn((m, d), generator=g, device=device, dtype=torch.float32) * math.sqrt(eig_lo)
-        out[pos:pos + m] = blk
-        pos += m
+        for c in range(c0, c1):
+            m = int(sizes[c])
+            if m == 0:
+                continue
+            z = torch.randn((m, d), generator=g, device=device, dtype=torch.float32) * eig[c - c0].sqrt()
+            out[pos:pos + m] = centres[c] * 0.5 + z @ basis[c - c0].T
+            pos += m
     out = out[torch.randperm(n, generator=g, device=device)]
     out /= out.double().norm(dim=1, keepdim=True).float()
     host = out.cpu().numpy()
@@ -382,7 +384,7 @@ def batch_instances(count: int = 2000, seed: int = 7, n_lo: int = 1_000,
         d = int(master.choice([2, 8, 18, 32, 57, 90]))
         nc = int(master.integers(1, 51))
         tgt = float(master.choice([4.0, 16.0, 64.0]))
-        pts = gen_clusters(n, d, nc, seed=seed * 100_003 + i, eig_lo=1e-2)
+        pts = gen_clusters(n, d, nc, seed=seed * 100_003 + i, eig_lo=1e-2, rank=32)
         eps = calibrate_eps(pts, tgt, sample=min(n, 4000), seed=i)
         out.append(Workload(f"batch{i}", pts, min(6, d), eps, tgt,
                             {"index": i}))

@@ -47,9 +47,9 @@ def gen_case(c: dict) -> np.ndarray:
     if g == "msd":
         return W.gen_msd_like(n, d, seed)
     if g == "clusters":
-        return W.gen_clusters(n, d, c.get("clusters", 8), seed, normalise=c.get("normalise", False))
+        return W.gen_clusters(n, d, c.get("clusters", 8), seed, normalise=c.get("normalise", False), rank=32)
     if g == "clusters_norm":
-        return W.gen_clusters(n, d, c.get("clusters", 8), seed, zipf=1.1, normalise=True)
+        return W.gen_clusters(n, d, c.get("clusters", 8), seed, zipf=1.1, normalise=True, rank=32)
     if g == "grid":
         rng = np.random.default_rng(seed)
         return rng.integers(0, c.get("side", 4), size=(n, d)).astype(np.float64)

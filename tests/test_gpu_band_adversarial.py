@@ -52,14 +52,23 @@ def shell_case(d: int, n_pairs: int, rho_max: float, seed: int):
     return x, rps
 
 
+@pytest.mark.parametrize("prec", ["auto", "bf16", "tf32"])
 @pytest.mark.parametrize("rho_max", [4.0, 12.0, 30.0])
 @pytest.mark.parametrize("d", [18, 90, 384])
-def test_pairs_around_the_band(handle, monkeypatch, d, rho_max):
+def test_pairs_around_the_band(handle, monkeypatch, d, rho_max, prec):
+    """prec: the library's choice in BF16 mode (split for short rows; split
+    or single bf16 for d = 384), single bf16 forced on the K-chunked kernel
+    (d = 384 only), or TF32 mode."""
+    if prec == "bf16" and d != 384:
+        pytest.skip("single bf16 operands exist on the K-chunked kernel only")
     monkeypatch.setenv("MISTIC_TC_MIN_BIN", "1")  # every home bin on the tensor cores
+    if prec == "bf16":
+        monkeypatch.setenv("MISTIC_TC_PREC", "bf16")
     x, rps = shell_case(d, 1500, rho_max, seed=d * 100 + int(rho_max))
     eps = 1.0
     ref = O.brute_pairs(x, eps)
-    r = handle.selfjoin(x, 2, eps, mode="bf16", rp="user", rp_user=rps, pairs="host", sort_pairs=True)
+    r = handle.selfjoin(x, 2, eps, mode="tf32" if prec == "tf32" else "bf16", rp="user", rp_user=rps,
+                        pairs="host", sort_pairs=True)
     assert r.n_units_tc > 0 and r.tc_tiles > 0
     assert r.band_pairs > 0
     assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)

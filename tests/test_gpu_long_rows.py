@@ -92,3 +92,54 @@ def test_repeat_calls_same_handle(handle):
     b = run(handle, x, 3, eps, mode="bf16")
     assert np.array_equal(a.pairs, b.pairs)
     assert np.array_equal(a.pairs, O.brute_pairs(x, eps))
+
+
+@pytest.mark.parametrize("prec", ["split", "bf16", "tf32"])
+@pytest.mark.parametrize("d", [130, 384])
+def test_operand_precisions(handle, monkeypatch, prec, d):
+    """The K-chunked join at each operand precision: split bf16 (3 products),
+    single bf16 (forced here; the library picks it only when its bound leaves
+    a narrow band) and tf32 (MISTIC_MODE_TF32).  Exact pair sets in all."""
+    monkeypatch.setenv("MISTIC_TC_MIN_BIN", "1")
+    rng = np.random.default_rng(d + 7)
+    x = rng.normal(size=(3000, d)).astype(np.float32)
+    x /= np.linalg.norm(x, axis=1, keepdims=True)
+    x[1500:] = x[:1500] + rng.normal(scale=0.02, size=(1500, d)).astype(np.float32)
+    eps = 0.3
+    ref = O.brute_pairs(x, eps)
+    assert len(ref) > 1000
+    if prec != "tf32":
+        monkeypatch.setenv("MISTIC_TC_PREC", prec)
+    r = run(handle, x, 4, eps, mode="tf32" if prec == "tf32" else "bf16")
+    assert r.mode_used == ("tf32" if prec == "tf32" else "bf16")
+    assert r.n_units == 0 and r.n_units_tc > 0
+    assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)
+
+
+@pytest.mark.parametrize("d", [8, 18, 57, 90])
+def test_tf32_mode_short_rows(handle, d):
+    """TF32 mode runs every tensor-core unit on the K-chunked kernel, short
+    rows included (globally centred rows; columns whose bound is too wide go
+    to FP64): exact pair sets."""
+    rng = np.random.default_rng(40 + d)
+    x = rng.normal(size=(6000, d))
+    eps = float(np.sqrt(d) * 0.35)
+    ref = O.brute_pairs(x, eps)
+    r = run(handle, x, 6, eps, mode="tf32")
+    assert r.mode_used == "tf32"
+    assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)
+
+
+def test_single_bf16_is_picked_for_wide_bands(handle):
+    """Unit-norm rows with eps comparable to their spread: the single-bf16
+    bound stays within eps^2 / 20, so AUTO runs a third of the tensor work;
+    the band is decided in FP64 and the pair set is exact."""
+    rng = np.random.default_rng(77)
+    x = rng.normal(size=(5000, 256)).astype(np.float32)
+    x /= np.linalg.norm(x, axis=1, keepdims=True)
+    x[2500:] = x[:2500] + rng.normal(scale=0.04, size=(2500, 256)).astype(np.float32)
+    eps = 1.0
+    ref = O.brute_pairs(x, eps)
+    r = run(handle, x, 8, eps)
+    assert r.mode_used == "bf16"
+    assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)

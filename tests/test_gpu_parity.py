@@ -12,7 +12,7 @@ from mistic import _lib as L
 
 pytestmark = pytest.mark.gpu
 
-MODES = ["auto", "fp64", "fp32", "bf16"]
+MODES = ["auto", "fp64", "fp32", "bf16", "tf32"]
 
 
 def run(h, x, k, eps, **kw):

@@ -1,8 +1,9 @@
 """Accuracy of the tensor-core arithmetic the joins' error band relies on.
 
 The band bound of the tensor-core joins (join_tc.cu, join_tcw.cu) allows for
-  - the operand rounding (split bf16: <= 3.02 * 2^-18 of |a_k||q_k| a product;
-    single bf16: 2^-8 + 2^-18; tf32 rounded to nearest: 2^-10 + 2^-22), and
+  - the operand rounding (bf16 keeps 8 significant bits, tf32 11; split
+    bf16: <= 3.02 * 2^-16 of |a_k||q_k| a product; single bf16:
+    2^-7 + 2^-16; tf32 rounded to nearest: 2^-10 + 2^-22), and
   - the FP32 accumulation in tensor memory: an allowance of 2^-19 of the sum
     of |products| per MMA instruction.
 The accumulation allowance is not a documented hardware property, so these
@@ -129,7 +130,7 @@ def test_tf32_reads_pre_rounded_operands_exactly():
 def test_split_bf16_product_error(K):
     """The joins' split-bf16 product on FP32 operands (hi.hi + hi.lo + lo.hi
     accumulated in one tile, 3 K/16 instructions) against the exact FP64
-    Gram of the FP32 values: within the operand allowance 3.02 * 2^-18 plus
+    Gram of the FP32 values: within the operand allowance 3.02 * 2^-16 plus
     the accumulation allowance."""
     rng = np.random.default_rng(K)
     a, b = operands(rng, K, "mixed")
@@ -141,7 +142,29 @@ def test_split_bf16_product_error(K):
     d = probe(0, A, B)
     ex, mag = exact_gram(a.astype(np.float64), b.astype(np.float64))
     n_inst = 3 * K // 16
-    bound = 3.02 * 2.0 ** -18 + n_inst * ALLOW_PER_INST
+    bound = 3.02 * 2.0 ** -16 + n_inst * ALLOW_PER_INST
     rel = float((np.abs(d - ex) / mag).max())
     print(f"split bf16 K={K}: max error {rel:.3e} of sum|a_k||b_k| (bound {bound:.3e})")
+    assert rel <= bound
+
+
+@pytest.mark.parametrize("kind", ["bf16", "tf32"])
+def test_single_operand_product_error(kind):
+    """Single-operand precisions of the K-chunked join on FP32 values (rows
+    rounded once to bf16 or to tf32) against the exact FP64 Gram: within the
+    operand allowance (bf16: 2^-7 + 2^-16, tf32: 2^-10 + 2^-22) plus the
+    accumulation allowance."""
+    K = 64
+    rng = np.random.default_rng(11 if kind == "bf16" else 12)
+    a, b = operands(rng, K, "mixed")
+    if kind == "bf16":
+        d = probe(0, to_bf16(a), to_bf16(b))
+        n_inst, op = K // 16, 2.0 ** -7 + 2.0 ** -16
+    else:
+        d = probe(1, to_tf32(a), to_tf32(b))
+        n_inst, op = K // 8, 2.0 ** -10 + 2.0 ** -22
+    ex, mag = exact_gram(a.astype(np.float64), b.astype(np.float64))
+    bound = op + n_inst * ALLOW_PER_INST
+    rel = float((np.abs(d - ex) / mag).max())
+    print(f"single {kind} K={K}: max error {rel:.3e} of sum|a_k||b_k| (bound {bound:.3e})")
     assert rel <= bound
