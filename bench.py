@@ -541,7 +541,8 @@ def run_north_star(h, args, dev, stream, peaks) -> dict:
         "band_fraction": r.band_pairs / max(1, r.candidates), "ulp_ambiguous": r.ulp_ambiguous,
         "distance_evals_per_s": r.candidates / (ms * 1e-3), "pairs_per_s": r.pairs_ij / (ms * 1e-3),
         "phase_ms": {k2: round(v, 3) for k2, v in r.ms.items()},
-        "bins": r.n_bins, "units_tc": r.n_units_tc, "tc_tiles": r.tc_tiles,
+        "bins": r.n_bins, "units": r.n_units, "units_tc": r.n_units_tc, "tc_tiles": r.tc_tiles,
+        "tc_min_bin": r.tc_min_bin, "tuned": r.tuned,
         "roofline": roof,
         "sample": {
             "home_sample": S, "candidates": qf.candidates, "pairs_ij": qf.pairs_ij,

@@ -125,6 +125,14 @@ typedef struct mistic_opts {
                                  candidates; counts, pair list and times cover that
                                  sample.  For comparing modes and tuning on a fixed
                                  subset of the work.  No counterpart in the reference. */
+  int32_t autotune;           /* tensor-core join tuning (bin threshold, operand precision),
+                                 timed on a sample of the work and cached per shape -- d,
+                                 dtype, kernel, bin-size histogram class, eps against the
+                                 rows' norms -- in memory and in the file MISTIC_TUNE_CACHE
+                                 (default $HOME/.cache/mistic/tune.tsv): 0 (default) for
+                                 joins of at least a million points, 1 always, -1 never.
+                                 Replaces the reference's compile-time tunables
+                                 (include/params.cuh:20-87). */
 } mistic_opts;
 
 typedef struct mistic_result {
@@ -158,6 +166,9 @@ typedef struct mistic_result {
   int32_t csr_on_device;
   int32_t tc_operands;              /* tensor-core operand precision used: 0 none, 1 split
                                        bf16 (hi/lo), 2 single bf16, 3 tf32 */
+  uint32_t tc_min_bin;              /* smallest home bin joined on the tensor cores */
+  int32_t tuned;                    /* 1: tc_min_bin / operands came from the autotuner
+                                       (measured now, or cached for this shape) */
   void* _owner;                     /* internal: non-NULL when the result owns `pairs` */
 } mistic_result;
 

@@ -611,6 +611,27 @@ void enumerate(mistic_handle_s* h, const uint64_t* bkey, const uint32_t* bstart,
   launched(h, fill ? "enum_fill" : "enum_count");
 }
 
+// Points per log2 bin-size class: hist[c] += size of every bin with
+// floor(log2(size)) == c (c < 32).
+__global__ void k_bin_hist(const uint32_t* __restrict__ bstart, uint32_t m, unsigned long long* __restrict__ hist) {
+  __shared__ unsigned long long sh[32];
+  if (threadIdx.x < 32) sh[threadIdx.x] = 0;
+  __syncthreads();
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < m; b += gridDim.x * blockDim.x) {
+    const uint32_t sz = bstart[b + 1] - bstart[b];
+    if (sz) atomicAdd(&sh[31 - __clz(sz)], (unsigned long long)sz);
+  }
+  __syncthreads();
+  if (threadIdx.x < 32 && sh[threadIdx.x]) atomicAdd(&hist[threadIdx.x], sh[threadIdx.x]);
+}
+
+void bin_hist(mistic_handle_s* h, const uint32_t* bstart, uint32_t m, unsigned long long* hist) {
+  MCK(cudaMemsetAsync(hist, 0, 32 * sizeof(unsigned long long), h->stream));
+  const unsigned nb = std::max(1u, std::min((m + 255) / 256, 4u * (unsigned)h->sms));
+  k_bin_hist<<<nb, 256, 0, h->stream>>>(bstart, m, hist);
+  launched(h, "bin_hist");
+}
+
 void count_totals(mistic_handle_s* h, const uint32_t* nbr_cnt, const uint32_t* unit_cnt, const uint32_t* unit_cnt_tc,
                   uint32_t m, unsigned long long* tot) {
   MCK(cudaMemsetAsync(tot, 0, 3 * sizeof(unsigned long long), h->stream));

@@ -227,6 +227,8 @@ void enumerate(mistic_handle_s*, const uint64_t* bkey, const uint32_t* bstart, u
                const EnumParams&, uint32_t* nbr_cnt, uint32_t* unit_cnt, uint32_t* unit_cnt_tc,
                unsigned long long* cand, const uint32_t* nbr_off, const uint32_t* unit_off,
                const uint32_t* unit_off_tc, uint32_t* nbr, Unit* units, Unit* units_tc, bool fill);
+// points per log2 bin-size class (32 classes) into hist
+void bin_hist(mistic_handle_s*, const uint32_t* bstart, uint32_t m, unsigned long long* hist);
 // 64-bit totals of the enumeration's three per-bin count arrays into tot[3]
 void count_totals(mistic_handle_s*, const uint32_t* nbr_cnt, const uint32_t* unit_cnt, const uint32_t* unit_cnt_tc,
                   uint32_t m, unsigned long long* tot);

@@ -27,8 +27,11 @@
 #include <atomic>
 #include <mutex>
 #include <thread>
+#include <functional>
 #include <unordered_map>
 #include <vector>
+
+#include <sys/stat.h>
 
 #include "internal.cuh"
 
@@ -373,6 +376,160 @@ void check_handle(mistic_handle h) {
   MCK(cudaSetDevice(h->device));
 }
 
+// ------------------------------------------------------------------ autotuner
+// The reference fixes its launch shape at compile time (include/params.cuh:
+// 20-87: TPP, ILP, KB, BS, CALC_PER_BATCH) and its batch plan by a formula
+// (src/launcher.cu:3202-3249).  Here the tensor-core join's two free choices
+// -- the smallest home bin it takes (smaller bins go to the CUDA-core join)
+// and, for the K-chunked kernel, split or single bf16 operands -- are timed
+// on a fixed sample of the actual work (mistic_opts.home_sample) the first
+// time a shape is seen, and cached.  Shape key: d, dtype, kernel, the
+// point-weighted bin-size histogram (classes of the median and the 90th
+// percentile point's bin), and log2(R^2 / eps^2) (how wide the band is
+// against the rows' norms).  Cache: in memory, and lines of
+// "key <TAB> tc_min <TAB> precision <TAB> ms" in MISTIC_TUNE_CACHE (default
+// $HOME/.cache/mistic/tune.tsv), read once per process.
+struct TuneCandidate {
+  uint32_t tc_min;
+  int prec;
+};
+struct Tuned {
+  uint32_t tc_min = 0;
+  int prec = 0;
+};
+
+class TuneCache {
+ public:
+  bool find(const std::string& key, Tuned* t) {
+    std::lock_guard<std::mutex> g(mu_);
+    load();
+    auto it = map_.find(key);
+    if (it == map_.end()) return false;
+    *t = it->second;
+    return true;
+  }
+  void put(const std::string& key, const Tuned& t, double ms) {
+    std::lock_guard<std::mutex> g(mu_);
+    load();
+    map_[key] = t;
+    const std::string path = file();
+    if (path.empty()) return;
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos && slash > 0) {  // create the directory (one level and its parent)
+      const std::string dir = path.substr(0, slash);
+      const size_t s2 = dir.rfind('/');
+      if (s2 != std::string::npos && s2 > 0) mkdir(dir.substr(0, s2).c_str(), 0755);
+      mkdir(dir.c_str(), 0755);
+    }
+    std::ofstream f(path, std::ios::app);
+    if (f) f << key << '\t' << t.tc_min << '\t' << t.prec << '\t' << ms << '\n';
+  }
+
+ private:
+  static std::string file() {
+    if (const char* e = getenv("MISTIC_TUNE_CACHE")) return std::string(e);
+    if (const char* hm = getenv("HOME")) return std::string(hm) + "/.cache/mistic/tune.tsv";
+    return std::string();
+  }
+  void load() {
+    if (loaded_) return;
+    loaded_ = true;
+    const std::string path = file();
+    if (path.empty()) return;
+    std::ifstream f(path);
+    std::string line;
+    while (std::getline(f, line)) {
+      const size_t a = line.find('\t');
+      if (a == std::string::npos) continue;
+      const size_t b = line.find('\t', a + 1);
+      if (b == std::string::npos) continue;
+      Tuned t;
+      t.tc_min = (uint32_t)strtoul(line.c_str() + a + 1, nullptr, 10);
+      t.prec = atoi(line.c_str() + b + 1);
+      if (t.tc_min >= 1 && t.prec >= 0 && t.prec <= 1) map_[line.substr(0, a)] = t;  // later lines win
+    }
+  }
+  std::mutex mu_;
+  bool loaded_ = false;
+  std::map<std::string, Tuned> map_;
+};
+
+TuneCache& tune_cache() {
+  static TuneCache* c = new TuneCache;
+  return *c;
+}
+
+using TuneMeasure = std::function<void(const TuneCandidate&, uint32_t sample, double* ms, unsigned long long* cands)>;
+
+// Looks the shape up, or times the candidates on a sample and records the
+// fastest.  Returns false when tuning is off (the defaults then stand).
+bool tune_lookup(mistic_handle_s* h, const mistic_opts& o, uint32_t d, mistic_dtype dt, bool wide, int prec_default,
+                 const uint32_t* bstart, uint32_t m, double eps2, double R, Tuned* out,
+                 const TuneMeasure& measure) {
+  int want = o.autotune;
+  if (const char* e = getenv("MISTIC_AUTOTUNE")) want = atoi(e) > 0 ? 1 : (atoi(e) < 0 || *e == '0' ? -1 : want);
+  if (want < 0) return false;
+  unsigned long long* hist_d = abuf<unsigned long long>(h, "tune_hist", 32);
+  idx::bin_hist(h, bstart, m, hist_d);
+  unsigned long long hist[32];
+  d2h(h, hist, hist_d, sizeof hist);
+  unsigned long long tot = 0;
+  for (int i = 0; i < 32; ++i) tot += hist[i];
+  if (want == 0 && tot < 1000000ull) return false;  // small joins: the defaults, no tuning cost
+  int c50 = 0, c90 = 0;
+  {
+    unsigned long long acc = 0;
+    bool got50 = false;
+    for (int i = 0; i < 32; ++i) {
+      acc += hist[i];
+      if (!got50 && 2 * acc >= tot) c50 = i, got50 = true;
+      if (10 * acc >= 9 * tot) {
+        c90 = i;
+        break;
+      }
+    }
+  }
+  const int eps_cls = (eps2 > 0 && R > 0) ? (int)std::floor(std::log2(R * R / eps2)) : 0;
+  char key[160];
+  snprintf(key, sizeof key, "v1 d=%u dt=%d %s bins=%d,%d r2e=%d", d, (int)dt, wide ? "tcw" : "tc", c50, c90, eps_cls);
+  if (tune_cache().find(key, out)) return true;
+  // candidates
+  std::vector<TuneCandidate> cands;
+  if (wide) {
+    std::vector<int> precs = {0};
+    if (prec_default == 1) precs.push_back(1);  // single bf16 only where its bound fits the cap
+    for (int pr : precs)
+      for (uint32_t t : {4u, 8u, 16u}) cands.push_back({t, pr});
+  } else {
+    const uint32_t t0 = tc_min_bin(d, false);
+    for (uint32_t t : {std::max(1u, t0 / 2), t0, std::min(512u, 2 * t0)})
+      if (cands.empty() || cands.back().tc_min != t) cands.push_back({t, 0});
+  }
+  // sample: about 1/64 of the home points; grown when one run takes long
+  uint32_t S = 64;
+  double best = 1e300;
+  Tuned bt{cands[0].tc_min, cands[0].prec};
+  for (size_t i = 0; i < cands.size(); ++i) {
+    double ms = 0;
+    unsigned long long cc = 0;
+    measure(cands[i], S, &ms, &cc);
+    if (i == 0 && ms > 150.0) {  // keep the tuning pass short: re-time on a smaller sample
+      S = (uint32_t)std::min(4096.0, S * ms / 100.0);
+      measure(cands[i], S, &ms, &cc);
+    }
+    if (getenv("MISTIC_DEBUG"))
+      fprintf(stderr, "[mistic] tune %s: tc_min=%u prec=%d sample 1/%u: %.3f ms (%llu candidates)\n", key,
+              cands[i].tc_min, cands[i].prec, S, ms, cc);
+    if (ms < best) {
+      best = ms;
+      bt = Tuned{cands[i].tc_min, cands[i].prec};
+    }
+  }
+  tune_cache().put(key, bt, best);
+  *out = bt;
+  return true;
+}
+
 // ------------------------------------------------------------------ the pipeline
 
 void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mistic_dtype dt, uint32_t k,
@@ -624,53 +781,50 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   ep.sample = o.home_sample;
   ep.tc_min = use_tc ? tc_min_bin(d, wide) : 0u;
   ep.tc_chunk = use_tc ? (wide ? 256u : join::tc_rows(d)) : 128;
-  uint32_t* nbr_cnt = abuf<uint32_t>(h, "nbr_cnt", m + 1);
-  uint32_t* unit_cnt = abuf<uint32_t>(h, "unit_cnt", m + 1);
-  uint32_t* unit_cnt_tc = abuf<uint32_t>(h, "unit_cnt_tc", m + 1);
-  unsigned long long* cand = abuf<unsigned long long>(h, "cand", m + 1);
-  idx::enumerate(h, bkey, bstart, m, ep, nbr_cnt, unit_cnt, unit_cnt_tc, cand, nullptr, nullptr, nullptr, nullptr,
-                 nullptr, nullptr, false);
-  uint32_t* tot32 = abuf<uint32_t>(h, "tot32", 3);
-  unsigned long long* tot64 = abuf<unsigned long long>(h, "tot64", 4);
-  // 64-bit totals first: the work lists index neighbours and units with
-  // 32-bit offsets, which a total of 2^32 or more would wrap
-  idx::count_totals(h, nbr_cnt, unit_cnt, unit_cnt_tc, m, tot64 + 1);
-  exclusive_scan<uint32_t>(h, nbr_cnt, nbr_cnt, m, tot32);
-  exclusive_scan<uint32_t>(h, unit_cnt, unit_cnt, m, tot32 + 1);
-  exclusive_scan<uint32_t>(h, unit_cnt_tc, unit_cnt_tc, m, tot32 + 2);
-  exclusive_scan<unsigned long long>(h, cand, cand, m, tot64);
-  uint32_t tots[3];
-  unsigned long long tot_all[4] = {0, 0, 0, 0};
-  d2h(h, tots, tot32, sizeof tots);
-  d2h(h, tot_all, tot64, sizeof tot_all);
-  const unsigned long long totc = tot_all[0];
-  {
+  uint32_t tots[3] = {0, 0, 0};
+  unsigned long long totc = 0;
+  uint32_t* nbr = nullptr;
+  Unit* units = nullptr;
+  Unit* units_tc = nullptr;
+  // count -> 64-bit totals check -> scans -> fill, into the arena's work lists
+  auto enumerate_units = [&](const EnumParams& e) {
+    uint32_t* nbr_cnt = abuf<uint32_t>(h, "nbr_cnt", m + 1);
+    uint32_t* unit_cnt = abuf<uint32_t>(h, "unit_cnt", m + 1);
+    uint32_t* unit_cnt_tc = abuf<uint32_t>(h, "unit_cnt_tc", m + 1);
+    unsigned long long* cand = abuf<unsigned long long>(h, "cand", m + 1);
+    idx::enumerate(h, bkey, bstart, m, e, nbr_cnt, unit_cnt, unit_cnt_tc, cand, nullptr, nullptr, nullptr, nullptr,
+                   nullptr, nullptr, false);
+    uint32_t* tot32 = abuf<uint32_t>(h, "tot32", 3);
+    unsigned long long* tot64 = abuf<unsigned long long>(h, "tot64", 4);
+    // 64-bit totals first: the work lists index neighbours and units with
+    // 32-bit offsets, which a total of 2^32 or more would wrap
+    idx::count_totals(h, nbr_cnt, unit_cnt, unit_cnt_tc, m, tot64 + 1);
+    exclusive_scan<uint32_t>(h, nbr_cnt, nbr_cnt, m, tot32);
+    exclusive_scan<uint32_t>(h, unit_cnt, unit_cnt, m, tot32 + 1);
+    exclusive_scan<uint32_t>(h, unit_cnt_tc, unit_cnt_tc, m, tot32 + 2);
+    exclusive_scan<unsigned long long>(h, cand, cand, m, tot64);
+    unsigned long long tot_all[4] = {0, 0, 0, 0};
+    d2h(h, tots, tot32, sizeof tots);
+    d2h(h, tot_all, tot64, sizeof tot_all);
+    totc = tot_all[0];
     // MISTIC_TEST_WORKLIST_LIMIT=k lowers the limit (tests of this check)
     unsigned long long lim = 0xffffffffull - 1;
-    if (const char* e = getenv("MISTIC_TEST_WORKLIST_LIMIT")) lim = std::min(lim, strtoull(e, nullptr, 10));
+    if (const char* ev = getenv("MISTIC_TEST_WORKLIST_LIMIT")) lim = std::min(lim, strtoull(ev, nullptr, 10));
     for (int i = 0; i < 3; ++i)
       if (tot_all[1 + i] > lim || tot_all[1 + i] != (unsigned long long)tots[i])
         throw Error(MISTIC_ERR_TOO_LARGE,
                     "neighbour-bin or work-unit list beyond the 32-bit offsets of the join work lists "
                     "(raise eps resolution: more reference points, or split the input)");
-  }
-  r->n_bin_pairs = tots[0];
-  r->n_units = tots[1];
-  r->n_units_tc = tots[2];
-  r->candidates = totc;
-  uint32_t* nbr = abuf<uint32_t>(h, "nbr", (size_t)tots[0] + 1);
-  Unit* units = abuf<Unit>(h, "units", (size_t)tots[1] + 1);
-  Unit* units_tc = abuf<Unit>(h, "units_tc", (size_t)tots[2] + 1);
-  idx::enumerate(h, bkey, bstart, m, ep, nullptr, nullptr, nullptr, nullptr, nbr_cnt, unit_cnt, unit_cnt_tc, nbr,
-                 units, units_tc, true);
-  clk.mark();  // 6
+    nbr = abuf<uint32_t>(h, "nbr", (size_t)tots[0] + 1);
+    units = abuf<Unit>(h, "units", (size_t)tots[1] + 1);
+    units_tc = abuf<Unit>(h, "units_tc", (size_t)tots[2] + 1);
+    idx::enumerate(h, bkey, bstart, m, e, nullptr, nullptr, nullptr, nullptr, nbr_cnt, unit_cnt, unit_cnt_tc, nbr,
+                   units, units_tc, true);
+  };
 
-  // ---- join
+  // ---- join parameters
   JoinParams jp{};
-  jp.units = units;
-  jp.n_units = tots[1];
   jp.bstart = bstart;
-  jp.nbr = nbr;
   jp.ids = ids;
   jp.xs = fp64 ? (const void*)xd : (const void*)xf;
   jp.dpad = fp64 ? dpad64 : dpad32;
@@ -682,19 +836,21 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   jp.eps2 = eps2;
   jp.amb = 4.0 * (nextafter(eps2, INFINITY) - eps2);
   JoinCounters* ctr = abuf<JoinCounters>(h, "ctr", 2);  // [0] CUDA-core join, [1] tensor-core cursor
+  jp.ctr = ctr;
   TcParams tp{};
-  if (use_tc) {
+  int prepared = -1;  // operand precision the K-chunked kernel's rows are prepared at
+  // tensor-core parameters at operand precision pr (rows prepared on demand)
+  auto set_tc = [&](int pr) {
+    if (!use_tc) return;
     const double u = ldexp(1.0, -24) * (1.0 + ldexp(1.0, -20));
     const double gd = d * u / (1.0 - d * u);
     const double g64 = (d + 2) * ldexp(1.0, -53) * 1.01;
-    tp.units = units_tc;
-    tp.n_units = tots[2];
     tp.ctr = ctr + 1;
     tp.eps2_lo = (float)(eps2 / (1.0 + g64));
     if ((double)tp.eps2_lo > eps2 / (1.0 + g64)) tp.eps2_lo = nextafterf(tp.eps2_lo, 0.f);
     tp.eps2_hi = (float)(eps2 / (1.0 - g64));
     if ((double)tp.eps2_hi < eps2 / (1.0 - g64)) tp.eps2_hi = nextafterf(tp.eps2_hi, INFINITY);
-    tp.kappa = (float)tc_kappa(d, wide, prec);
+    tp.kappa = (float)tc_kappa(d, wide, pr);
     tp.ginf = (float)(1.0 / (1.0 - gd) * (1.0 + 1e-6));
     tp.uR2 = (float)(2.0 * u * R * 1.0001);
     tp.u1 = (float)(u * (1.0 + u) * 1.0001);
@@ -708,20 +864,100 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     tp.stall_test = (st && *st == '1') ? 1 : 0;
     tp.wait_limit = tp.stall_test ? 2000000ll : 2000000000ll;  // 2 ms in the test, else 2 s
     tp.prof = getenv("MISTIC_DEBUG") ? 1 : 0;
-    tp.prec = prec;
-    if (wide && tots[2] > 0) {
-      tp.kd = join::tcw_kd(d, prec);
+    tp.prec = pr;
+    if (wide && prepared != pr) {
+      tp.kd = join::tcw_kd(d, pr);
       // operand rows: bf16 (hi, and lo for the split) or tf32 in FP32 words
-      void* xh = h->arena.get("xh", n * (size_t)tp.kd * (prec == 2 ? 4 : 2));
-      void* xl = prec == 0 ? h->arena.get("xl", n * (size_t)tp.kd * 2) : nullptr;
+      void* xh = h->arena.get("xh", n * (size_t)tp.kd * (pr == 2 ? 4 : 2));
+      void* xl = pr == 0 ? h->arena.get("xl", n * (size_t)tp.kd * 2) : nullptr;
       float* xn = abuf<float>(h, "xn", n);
-      join::tcw_prepare(h, prec, xf, dpad32, d, n, xh, xl, xn);
+      join::tcw_prepare(h, pr, xf, dpad32, d, n, xh, xl, xn);
       tp.xh = xh;
       tp.xl = xl;
       tp.xn = xn;
       tp.n_rows = n;
+      prepared = pr;
+    }
+  };
+  auto point_lists = [&]() {
+    jp.units = units;
+    jp.n_units = tots[1];
+    jp.nbr = nbr;
+    tp.units = units_tc;
+    tp.n_units = tots[2];
+  };
+  // one pass of the join kernels: CUDA cores, tensor cores, FP64 band decisions
+  auto launch_join = [&](bool timed) {
+    MCK(cudaMemsetAsync(ctr, 0, 2 * sizeof(JoinCounters), h->stream));
+    if (timed) MCK(cudaEventRecord(h->jev[0], h->stream));
+    join::run(h, fp64, CH, jp);
+    if (timed) MCK(cudaEventRecord(h->jev[1], h->stream));
+    if (use_tc) {
+      if (wide)
+        join::run_tcw(h, jp, tp);
+      else
+        join::run_tc(h, jp, tp);
+    }
+    if (timed) MCK(cudaEventRecord(h->jev[2], h->stream));
+    join::run_band(h, jp);
+    if (timed) MCK(cudaEventRecord(h->jev[3], h->stream));
+  };
+  // band list: pairs the FP32 / tensor-core joins leave to the FP64 check
+  auto size_band = [&](unsigned long long cands) {
+    if (fp64) return;
+    // measured band fractions are ~2e-5 - 5e-5 of the candidate pairs; start
+    // above that so the first call rarely has to run the join again
+    unsigned long long bcap = std::max<unsigned long long>(1ull << 20, 2ull * n);
+    bcap = std::max<unsigned long long>(bcap, std::min<unsigned long long>(cands / 8192, 1ull << 30));
+    auto it = h->arena.bufs.find("band");
+    if (it != h->arena.bufs.end()) bcap = std::max<unsigned long long>(bcap, it->second.bytes / 8);
+    // MISTIC_BAND_CAP=k starts from a k-entry list (tests of the overflow path)
+    if (const char* e = getenv("MISTIC_BAND_CAP")) bcap = std::max<unsigned long long>(1, strtoull(e, nullptr, 10));
+    jp.band_list = abuf<unsigned long long>(h, "band", bcap);
+    jp.band_cap = bcap;
+  };
+
+  // ---- autotuner: tensor-core bin threshold (and, for the K-chunked kernel,
+  // the operand precision) timed on a sample of the work, once per shape
+  int prec_used = prec;
+  if (use_tc && !tf32_mode) {
+    Tuned tu;
+    if (tune_lookup(h, o, d, dt, wide, prec, bstart, m, eps2, R, &tu, [&](const TuneCandidate& c, uint32_t S,
+                                                                           double* ms_out, unsigned long long* cands) {
+          EnumParams e2 = ep;
+          e2.tc_min = c.tc_min;
+          e2.sample = std::max<uint32_t>(S, o.home_sample);
+          enumerate_units(e2);
+          set_tc(c.prec);
+          point_lists();
+          jp.pairs = nullptr;
+          jp.cap = 0;
+          size_band(totc);
+          launch_join(true);
+          JoinCounters hc2{};
+          d2h(h, &hc2, ctr, sizeof hc2);
+          if (hc2.error) throw Error(MISTIC_ERR_TIMEOUT, "a tensor-core tile wait timed out");
+          float t = 0;
+          MCK(cudaEventElapsedTime(&t, h->jev[0], h->jev[3]));
+          *ms_out = t;
+          *cands = totc;
+        })) {
+      ep.tc_min = tu.tc_min;
+      prec_used = tu.prec;
+      r->tuned = 1;
     }
   }
+  r->tc_min_bin = ep.tc_min;
+  enumerate_units(ep);
+  r->n_bin_pairs = tots[0];
+  r->n_units = tots[1];
+  r->n_units_tc = tots[2];
+  r->candidates = totc;
+  clk.mark();  // 6
+
+  // ---- join
+  set_tc(prec_used);
+  point_lists();
   const bool want_pairs = o.pairs != MISTIC_PAIRS_NONE;
   const bool want_csr = o.csr != MISTIC_PAIRS_NONE;
   const bool need_pairs = want_pairs || want_csr;  // the CSR table is built from the pair list
@@ -741,38 +977,14 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   }
   jp.pairs = pbuf;
   jp.cap = cap;
-  jp.ctr = ctr;
-  // band list: pairs the FP32 / tensor-core joins leave to the FP64 check
-  if (!fp64) {
-    // measured band fractions are ~2e-5 - 5e-5 of the candidate pairs; start
-    // above that so the first call rarely has to run the join again
-    unsigned long long bcap = std::max<unsigned long long>(1ull << 20, 2ull * n);
-    bcap = std::max<unsigned long long>(bcap, std::min<unsigned long long>(totc / 8192, 1ull << 30));
-    auto it = h->arena.bufs.find("band");
-    if (it != h->arena.bufs.end()) bcap = std::max<unsigned long long>(bcap, it->second.bytes / 8);
-    // MISTIC_BAND_CAP=k starts from a k-entry list (tests of the overflow path)
-    if (const char* e = getenv("MISTIC_BAND_CAP")) bcap = std::max<unsigned long long>(1, strtoull(e, nullptr, 10));
-    jp.band_list = abuf<unsigned long long>(h, "band", bcap);
-    jp.band_cap = bcap;
-  }
+  size_band(totc);
   JoinCounters hc{};
   // MISTIC_TEST_JOIN_ATTEMPTS=k caps the passes (tests of the exit check below)
   int attempts = 3;
   if (const char* e = getenv("MISTIC_TEST_JOIN_ATTEMPTS")) attempts = std::max(1, atoi(e));
   bool complete = false;
   for (int attempt = 0; attempt < attempts; ++attempt) {
-    MCK(cudaMemsetAsync(ctr, 0, 2 * sizeof(JoinCounters), h->stream));
-    if (o.timing) MCK(cudaEventRecord(h->jev[0], h->stream));
-    join::run(h, fp64, CH, jp);
-    if (o.timing) MCK(cudaEventRecord(h->jev[1], h->stream));
-    if (use_tc) {
-      if (wide)
-        join::run_tcw(h, jp, tp);
-      else
-        join::run_tc(h, jp, tp);
-    }
-    if (o.timing) MCK(cudaEventRecord(h->jev[2], h->stream));
-    join::run_band(h, jp);
+    launch_join(o.timing != 0);
     d2h(h, &hc, ctr, sizeof hc);
     if (hc.error) throw Error(MISTIC_ERR_TIMEOUT, "a tensor-core tile wait timed out");
     if (hc.band_n > jp.band_cap) {  // band list overflowed: nothing beyond it was decided, run again
@@ -798,7 +1010,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   r->pairs_ordered_incl_self = 2 * hc.pairs + n;
   r->band_pairs = fp64 ? 0 : hc.band;
   r->ulp_ambiguous = hc.ambiguous;
-  r->tc_operands = (use_tc && tots[2] > 0) ? (wide ? 1 + prec : 1) : 0;
+  r->tc_operands = (use_tc && tots[2] > 0) ? (wide ? 1 + prec_used : 1) : 0;
   if (use_tc) {
     JoinCounters tcc{};
     d2h(h, &tcc, ctr + 1, sizeof tcc);

@@ -54,6 +54,8 @@ class JoinResult:
     csr_nbrs: np.ndarray | None = None       # (offsets[n],) uint32
     device_pairs: int | None = None          # device pointer when pairs="device"
     tc_operands: str = "none"                # tensor-core operands: none, split-bf16, bf16, tf32
+    tc_min_bin: int = 0                      # smallest home bin on the tensor cores
+    tuned: bool = False                      # threshold / operands from the autotuner
     extra: dict = field(default_factory=dict)
 
 
@@ -93,7 +95,7 @@ class Handle:
 
     def opts(self, mode="auto", rp="pca", seed=0, pairs="none", sort_pairs=False,
              pair_capacity=0, input_on_device=False, check_finite=True, timing=True,
-             rp_user=None, pair_buffer=None, csr="none", home_sample=0) -> L.Opts:
+             rp_user=None, pair_buffer=None, csr="none", home_sample=0, autotune=0) -> L.Opts:
         o = L.Opts()
         self.lib.mistic_opts_init(ctypes.byref(o))
         o.mode = MODES[mode]
@@ -109,6 +111,7 @@ class Handle:
         o.timing = 1 if timing else 0
         o.csr = {"none": L.PAIRS_NONE, "host": L.PAIRS_HOST, "device": L.PAIRS_DEVICE}[csr]
         o.home_sample = home_sample
+        o.autotune = autotune
         if rp_user is not None:
             self._rp_keep = np.ascontiguousarray(rp_user, dtype=np.float64)
             o.rp_user = self._rp_keep.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
@@ -153,7 +156,8 @@ class Handle:
             mode_used={0: "auto", 1: "fp64", 2: "fp32", 3: "bf16", 4: "tf32"}.get(r.mode_used, "?"),
             ms=ms, kernel_launches=r.kernel_launches, pairs=pairs, device_pairs=dev,
             csr_offsets=csr_off, csr_nbrs=csr_nb,
-            tc_operands={0: "none", 1: "split-bf16", 2: "bf16", 3: "tf32"}.get(r.tc_operands, "?"))
+            tc_operands={0: "none", 1: "split-bf16", 2: "bf16", 3: "tf32"}.get(r.tc_operands, "?"),
+            tc_min_bin=r.tc_min_bin, tuned=bool(r.tuned))
         if not keep_device or not r.pairs_on_device:
             self.lib.mistic_result_free(ctypes.byref(r))
         else:

@@ -54,6 +54,7 @@ class Opts(ctypes.Structure):
         ("timing", i32),
         ("csr", i32),
         ("home_sample", u32),
+        ("autotune", i32),
     ]
 
 
@@ -86,6 +87,8 @@ class Result(ctypes.Structure):
         ("csr_nbrs", ctypes.POINTER(u32)),
         ("csr_on_device", i32),
         ("tc_operands", i32),
+        ("tc_min_bin", u32),
+        ("tuned", i32),
         ("_owner", vp),
     ]
 

@@ -104,7 +104,7 @@ def test_operand_precisions(handle, monkeypatch, prec, d):
     rng = np.random.default_rng(d + 7)
     x = rng.normal(size=(3000, d)).astype(np.float32)
     x /= np.linalg.norm(x, axis=1, keepdims=True)
-    x[1500:] = x[:1500] + rng.normal(scale=0.02, size=(1500, d)).astype(np.float32)
+    x[1500:] = x[:1500] + rng.normal(scale=0.25 / np.sqrt(d), size=(1500, d)).astype(np.float32)
     eps = 0.3
     ref = O.brute_pairs(x, eps)
     assert len(ref) > 1000
@@ -139,6 +139,7 @@ def test_single_bf16_is_picked_for_wide_bands(handle):
     x /= np.linalg.norm(x, axis=1, keepdims=True)
     x[2500:] = x[:2500] + rng.normal(scale=0.04, size=(2500, 256)).astype(np.float32)
     eps = 1.0
+    # single bf16 fits the cap here: |a| + |q| <= 2 + noise, eps^2 = 1
     ref = O.brute_pairs(x, eps)
     r = run(handle, x, 8, eps)
     assert r.mode_used == "bf16"
