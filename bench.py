@@ -619,9 +619,16 @@ def run_batch(args) -> None:
     clocks.start()
     ms, res = timed(inst_d, o_cnt, args.steps)
     clk = clocks.stop()
+    # the same batch with one pipeline per instance: on 8 worker streams, and
+    # one instance after another (one launch of each join kernel per instance)
+    os.environ["MISTIC_BATCH_FUSED"] = "0"
+    batch(inst_d, o_cnt)
+    streams_ms, res_s = timed(inst_d, o_cnt, 1)
     os.environ["MISTIC_BATCH_STREAMS"] = "1"
     serial_ms, _ = timed(inst_d, o_cnt, 1)
     del os.environ["MISTIC_BATCH_STREAMS"]
+    del os.environ["MISTIC_BATCH_FUSED"]
+    counts_same = [p[0] for p in res] == [p[0] for p in res_s]
     o_host = h.opts(pairs="host", mode=args.mode)
     batch(inst_h, o_host)
     e2e_ms, _ = timed(inst_h, o_host, args.steps)
@@ -666,11 +673,15 @@ def run_batch(args) -> None:
                    "desc": "2,000 instances, n log-uniform [1e3,2e5], d in {2,8,18,32,57,90}, FP32 "
                            "Gaussian mixtures, 4/16/64 mean neighbours", "mode": args.mode,
                    "parallelism": "replicas" if world > 1 else "single",
-                   "streams": "worker handles (MISTIC_BATCH_STREAMS default)", "pairs_to": "counts only",
+                   "streams": "index builds on worker handles; the join of all instances fused into one "
+                              "persistent launch per (kernel, d) class, captured as one CUDA graph",
+                   "pairs_to": "counts only",
                    "timing": "host clock around the synchronous batch call, device synchronised",
                    "l2": f"inputs {sum(x.nbytes for x in xs) / 1e9:.1f} GB in total"},
         "pairs_ij": pairs, "candidates": sum(p[2] for p in res),
-        "serial_ms_per_step": serial_ms, "stream_speedup": serial_ms / ms,
+        "per_instance_streams_ms_per_step": streams_ms, "per_instance_serial_ms_per_step": serial_ms,
+        "fused_vs_serial": serial_ms / ms, "fused_vs_streams": streams_ms / ms,
+        "counts_identical_fused_vs_per_instance": counts_same,
         "generation_s": t_gen, "parity": parity,
         "roofline": None,
         "e2e": {"value": world * tot_n / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,

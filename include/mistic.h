@@ -133,6 +133,22 @@ typedef struct mistic_opts {
                                  joins of at least a million points, 1 always, -1 never.
                                  Replaces the reference's compile-time tunables
                                  (include/params.cuh:20-87). */
+  uint64_t ring_capacity;     /* 0 (default): one pair list sized to the result.  R > 0: pairs
+                                 stream through a device ring of R pairs (the reference keeps
+                                 a fixed 2.5e9-pair buffer, src/launcher.cu:3340-3349, and
+                                 nodeByPoint4 stops at 80 % of it, src/kernel.cu:912-989):
+                                 when the ring fills, the join stops claiming work units, the
+                                 ring is drained to the host (or to pair_sink), and the join
+                                 resumes from its work cursor.  A unit that lost pairs to the
+                                 full ring runs again in the next pass; its partial pairs are
+                                 dropped (result.ring_units_redone).  Needs pairs = HOST or a
+                                 pair_sink; no CSR table.  MISTIC_ERR_PAIR_OVERFLOW when one
+                                 work unit alone has more pairs than the ring holds. */
+  void (*pair_sink)(const uint32_t* pairs, uint64_t count, void* user);
+                              /* ring mode: called on the calling thread with each drained
+                                 batch of `count` pairs (i, j), i < j, in host memory valid
+                                 for the call only; the result then holds no pair list */
+  void* sink_user;
 } mistic_opts;
 
 typedef struct mistic_result {
@@ -169,6 +185,8 @@ typedef struct mistic_result {
   uint32_t tc_min_bin;              /* smallest home bin joined on the tensor cores */
   int32_t tuned;                    /* 1: tc_min_bin / operands came from the autotuner
                                        (measured now, or cached for this shape) */
+  uint32_t ring_passes;             /* ring mode: join passes (ring drains) */
+  uint64_t ring_units_redone;       /* ring mode: units run again after the ring filled */
   void* _owner;                     /* internal: non-NULL when the result owns `pairs` */
 } mistic_result;
 

@@ -80,6 +80,8 @@ struct JoinCounters {
   unsigned long long tiles;      // tensor-core tiles evaluated
   unsigned long long cells;      // sum over those tiles of home rows x candidate columns
   unsigned long long band_n;     // candidate pairs appended to the band list (decided afterwards in FP64)
+  unsigned long long stop;       // pair ring: a list was full; no unit is claimed after it
+  unsigned long long def_n;      // pair ring: units deferred in this pass
   unsigned long long prof[24];   // role cycle breakdown when TcParams.prof is set
 };
 
@@ -107,6 +109,37 @@ struct EnumParams {
   uint32_t sample;   // > 1: only home points of sampled 512-point groups (mistic_opts.home_sample)
 };
 
+// FP32 constants of a tensor-core join's per-column error bound (see
+// column_threshold in tc_common.cuh).
+struct TcBound {
+  float eps2_lo, eps2_hi;  // fl32 bounds of eps2/(1+g64), eps2/(1-g64)
+  float kappa;             // relative MMA + norm error per (|a'|+|q'|)^2
+  float ginf;              // norm inflation 1/(1-g_d)
+  float uR2;               // 2uR (global centring error)
+  float u1;                // u(1+u)
+  float Dp;                // 1.1 sqrt(eps2)
+  float cap;               // 0.1 eps2: larger bounds re-decide the whole column in FP64
+  float margin;            // small positive slack that makes D' >= 0 a strict reject
+};
+
+// One instance of a fused batch join (mistic_batch_selfjoin): its sorted
+// rows, bins and neighbour list, and its thresholds.  Join kernels given
+// JoinParams.insts take each unit's instance from unit_inst and read these
+// in place of the single-instance fields; ids are global (row0 + the
+// instance's own row id), so pairs of different instances never collide.
+struct InstDesc {
+  const uint32_t* bstart;
+  const uint32_t* nbr;
+  const uint32_t* ids;
+  const void* xs;      // sorted FP32 rows, stride dpad of the launch
+  const void* raw;     // the instance's rows as given (device), for the FP64 decisions
+  uint32_t d, raw_f32;
+  uint32_t row0;       // first global row id of the instance
+  float t_lo, t_hi;    // FP32 filter
+  double eps2, amb;
+  TcBound tcb;         // tensor-core bound
+};
+
 struct JoinParams {
   const Unit* units;
   unsigned long long n_units;
@@ -126,6 +159,34 @@ struct JoinParams {
   unsigned long long* band_list;  // packed (i << 32 | j) original ids whose fast value is inside the error band
   unsigned long long band_cap;
   JoinCounters* ctr;
+  // fused batch joins only (null otherwise)
+  const InstDesc* insts;             // per instance
+  const uint32_t* unit_inst;         // instance of each unit of `units`
+  const uint32_t* inst_row0;         // insts[i].row0, ascending (band decisions find a pair's instance)
+  uint32_t n_inst;
+  unsigned long long* inst_pairs;    // accepted pairs per instance
+  // streamed pair ring only (mistic_opts.ring_capacity; `ring` 0 otherwise).
+  // A launch claims the units def_in[0 .. n_def_in) (deferred by the last
+  // pass), then main_start, main_start + 1, ... of its own list; unit u of
+  // the CUDA-core list has tag u, unit u of the tensor-core list tag
+  // n_units + u (tag_base_tc).
+  int ring;
+  uint32_t* pair_tags;               // unit tag of each pair-ring entry
+  uint32_t* band_tags;               // unit tag of each band-list entry
+  uint32_t* deferred;                // per tag: 1 once deferred in this pass
+  uint32_t* def_out;                 // tags deferred in this pass (count in ctr->def_n)
+  const uint32_t* def_in;            // CUDA-core list: units to run first (local indices)
+  uint32_t n_def_in;
+  unsigned long long main_start;     // CUDA-core list: first unit not yet claimed
+  uint32_t tag_base_tc;
+  unsigned long long band0, band1;   // band decisions of band_list[band0 .. band1) (pair ring)
+  uint32_t grid_cap;                 // pair ring: at most this many blocks (0: the persistent grid)
+  // FP32 pre-decision of band pairs (null inv: every band pair goes to FP64):
+  // rows xf32[inv[id]] (sorted FP32 rows, stride dpad32) filtered with the
+  // FP32 filter's thresholds t_lo / t_hi before the FP64 predicate
+  const uint32_t* inv;
+  const float* xf32;
+  uint32_t dpad32;
 };
 
 // Tensor-core join: FP32 constants of the per-row error bound (see join_tc.cu).
@@ -133,14 +194,12 @@ struct TcParams {
   const Unit* units;
   unsigned long long n_units;
   JoinCounters* ctr;  // separate cursor from the CUDA-core join
-  float eps2_lo, eps2_hi;  // fl32 bounds of eps2/(1+g64), eps2/(1-g64)
-  float kappa;             // relative MMA + norm error per (|a'|+|q'|)^2
-  float ginf;              // norm inflation 1/(1-g_d)
-  float uR2;               // 2uR (global centring error)
-  float u1;                // u(1+u)
-  float Dp;                // 1.1 sqrt(eps2)
-  float cap;               // 0.1 eps2: larger bounds re-decide the whole column in FP64
-  float margin;            // small positive slack that makes D' >= 0 a strict reject
+  const uint32_t* unit_inst;  // fused batch joins: instance of each unit (JoinParams.insts), else null
+  const uint32_t* def_in;     // pair ring: units to run first (local indices of `units`)
+  uint32_t n_def_in;
+  unsigned long long main_start;  // pair ring: first unit of `units` not yet claimed
+  uint32_t grid_cap;          // pair ring: at most this many CTAs (0: one per SM)
+  TcBound b;               // per-column bound constants (per instance in fused batch joins)
   long long wait_limit;    // nanoseconds before a barrier wait gives up
   int stall_test;          // failure-detection test: the MMA warp never signals (waits run out)
   int prof;                // record per-role wait/total cycles into ctr->prof (diagnostics)

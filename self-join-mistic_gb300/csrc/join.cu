@@ -44,32 +44,33 @@ __device__ __forceinline__ uint32_t warp_incl_scan_u32(uint32_t x) {
 }
 
 // The reference predicate (src/utils.cu:296-309): sequential, each of the
-// subtraction, product and sum rounded to FP64 (no contraction).
-__device__ __forceinline__ double exact_sqdist(const JoinParams& P, uint32_t i, uint32_t j) {
+// subtraction, product and sum rounded to FP64 (no contraction), on rows i
+// and j of the caller's row-major array `raw` (FP32 or FP64, d columns).
+__device__ __forceinline__ double exact_sqdist(const void* raw, int raw_f32, uint32_t d, uint32_t i, uint32_t j) {
   double s = 0.0;
   // loads in groups of 8 (all in flight), sums in coordinate order
-  for (uint32_t t0 = 0; t0 < P.d; t0 += 8) {
+  for (uint32_t t0 = 0; t0 < d; t0 += 8) {
     double av[8], bv[8];
-    if (P.raw_f32) {
-      const float* a = (const float*)P.raw + (size_t)i * P.d;
-      const float* b = (const float*)P.raw + (size_t)j * P.d;
+    if (raw_f32) {
+      const float* a = (const float*)raw + (size_t)i * d;
+      const float* b = (const float*)raw + (size_t)j * d;
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        av[k] = t0 + k < P.d ? (double)a[t0 + k] : 0.0;
-        bv[k] = t0 + k < P.d ? (double)b[t0 + k] : 0.0;
+        av[k] = t0 + k < d ? (double)a[t0 + k] : 0.0;
+        bv[k] = t0 + k < d ? (double)b[t0 + k] : 0.0;
       }
     } else {
-      const double* a = (const double*)P.raw + (size_t)i * P.d;
-      const double* b = (const double*)P.raw + (size_t)j * P.d;
+      const double* a = (const double*)raw + (size_t)i * d;
+      const double* b = (const double*)raw + (size_t)j * d;
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        av[k] = t0 + k < P.d ? a[t0 + k] : 0.0;
-        bv[k] = t0 + k < P.d ? b[t0 + k] : 0.0;
+        av[k] = t0 + k < d ? a[t0 + k] : 0.0;
+        bv[k] = t0 + k < d ? b[t0 + k] : 0.0;
       }
     }
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-      if (t0 + k < P.d) {
+      if (t0 + k < d) {
         const double df = __dsub_rn(av[k], bv[k]);
         s = __dadd_rn(s, __dmul_rn(df, df));
       }
@@ -78,24 +79,109 @@ __device__ __forceinline__ double exact_sqdist(const JoinParams& P, uint32_t i, 
   return s;
 }
 
+// What a join kernel needs about the instance of one unit: the launch's own
+// arrays, or in a fused batch join those of the unit's instance.
+struct UnitView {
+  const uint32_t* bstart;
+  const uint32_t* nbr;
+  const uint32_t* ids;
+  const void* xs;
+  float t_lo, t_hi;
+  double eps2, amb;
+  uint32_t inst;
+};
+
+// The pair-ring contexts of a launch (null pointers outside ring mode).
+struct RingPair {
+  RingCtx pairs, band;
+};
+__device__ __forceinline__ RingPair ring_ctx(const JoinParams& P) {
+  RingPair r;
+  r.pairs = RingCtx{P.pair_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
+  r.band = RingCtx{P.band_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
+  return r;
+}
+
+// Unit of claim index t of a CUDA-core launch: first the units deferred by
+// the last ring pass, then the list from main_start (the identity outside
+// ring mode).  In ring mode a unit claimed after the stop is deferred unrun.
+// Returns false when the worker has nothing more to do.
+__device__ __forceinline__ bool claim_unit(const JoinParams& P, const RingCtx* rc, unsigned long long t,
+                                           unsigned long long* u) {
+  unsigned long long v;
+  if (t < P.n_def_in) {
+    v = P.def_in[t];
+  } else {
+    v = P.main_start + (t - P.n_def_in);
+    if (v >= P.n_units) return false;
+  }
+  if (rc && *(volatile unsigned long long*)&P.ctr->stop) {
+    ring_defer(rc, (uint32_t)v);
+    return false;
+  }
+  *u = v;
+  return true;
+}
+
+// Warp-uniform claim: lane 0 takes the next claim index.
+__device__ __forceinline__ bool warp_claim(const JoinParams& P, const RingCtx* rc, unsigned long long* u) {
+  unsigned long long v = ~0ull;
+  if ((threadIdx.x & 31) == 0) {
+    const unsigned long long t = atomicAdd(&P.ctr->next_unit, 1ull);
+    if (!claim_unit(P, rc, t, &v)) v = ~0ull;
+  }
+  v = __shfl_sync(FULL_MASK, v, 0);
+  *u = v;
+  return v != ~0ull;
+}
+
+__device__ __forceinline__ UnitView unit_view(const JoinParams& P, unsigned long long u) {
+  UnitView v;
+  if (P.insts) {
+    v.inst = P.unit_inst[u];
+    const InstDesc& I = P.insts[v.inst];
+    v.bstart = I.bstart;
+    v.nbr = I.nbr;
+    v.ids = I.ids;
+    v.xs = I.xs;
+    v.t_lo = I.t_lo;
+    v.t_hi = I.t_hi;
+    v.eps2 = I.eps2;
+    v.amb = I.amb;
+  } else {
+    v.inst = 0;
+    v.bstart = P.bstart;
+    v.nbr = P.nbr;
+    v.ids = P.ids;
+    v.xs = P.xs;
+    v.t_lo = P.t_lo;
+    v.t_hi = P.t_hi;
+    v.eps2 = P.eps2;
+    v.amb = P.amb;
+  }
+  if (P.ring) v.inst = (uint32_t)u;  // the ring's tag of the unit's pairs (no fused batch in ring mode)
+  return v;
+}
+
 // Stages this lane's pairs (bit a of `acc`: home point a0 + a with
 // candidate q) through the warp's buffer into a pair list (accepted pairs,
 // or the band list of pairs to re-decide in FP64).
-__device__ __forceinline__ void stage_hits(PairStage& ps, const JoinParams& P, uint32_t acc, uint32_t a0, uint32_t q,
+__device__ __forceinline__ void stage_hits(PairStage& ps, const uint32_t* ids, uint32_t acc, uint32_t a0, uint32_t q,
                                            unsigned long long* counter, unsigned long long* list,
-                                           unsigned long long cap) {
-  const uint32_t iq = acc ? P.ids[q] : 0u;
+                                           unsigned long long cap, unsigned long long* inst_pairs, uint32_t inst,
+                                           const RingCtx* rc) {
+  const uint32_t iq = acc ? ids[q] : 0u;
   uint32_t bits = acc;
   stage_pairs(
       ps, __popc(acc),
       [&](uint32_t) {
         const int a = __ffs(bits) - 1;
         bits &= bits - 1;
-        const uint32_t ia = P.ids[a0 + a];
+        const uint32_t ia = ids[a0 + a];
         const uint32_t lo = ia < iq ? ia : iq, hi = ia < iq ? iq : ia;
         return ((unsigned long long)lo << 32) | hi;
       },
-      counter, list, cap);
+      counter, list, cap, inst_pairs, inst, rc);
 }
 
 __device__ __forceinline__ void add_counter(unsigned long long* c, uint32_t v) {
@@ -128,14 +214,15 @@ struct CandTile {
   bool qv;
 };
 
-__device__ __forceinline__ CandTile next_tile(const JoinParams& P, uint32_t& s, uint32_t& off, uint32_t s1) {
+__device__ __forceinline__ CandTile next_tile(const uint32_t* nbr, const uint32_t* bstart, uint32_t& s, uint32_t& off,
+                                              uint32_t s1) {
   const int lane = threadIdx.x & 31;
   const uint32_t bj = s + lane;
   uint32_t start = 0, size = 0;
   if (bj < s1) {
-    const uint32_t b = P.nbr[bj];
-    start = P.bstart[b];
-    size = P.bstart[b + 1] - start;
+    const uint32_t b = nbr[bj];
+    start = bstart[b];
+    size = bstart[b + 1] - start;
     if (lane == 0) {
       start += off;
       size -= off;
@@ -222,14 +309,16 @@ k_join_f32(const JoinParams P) {
   unsigned long long* stg = reinterpret_cast<unsigned long long*>(smem_f4 + (size_t)(blockDim.x >> 5) * CH * nq4);
   PairStage ps{stg + (size_t)w * PSTAGE, 0};
   PairStage bs{stg + (size_t)((blockDim.x >> 5) + w) * PSTAGE, 0};
-  const float4* X = (const float4*)P.xs;
+  const RingPair RP = ring_ctx(P);
+  const RingCtx* rcp = P.ring ? &RP.pairs : nullptr;
+  const RingCtx* rcb = P.ring ? &RP.band : nullptr;
   for (;;) {
     unsigned long long u = 0;
-    if (lane == 0) u = atomicAdd(&P.ctr->next_unit, 1ull);
-    u = __shfl_sync(FULL_MASK, u, 0);
-    if (u >= P.n_units) break;
+    if (!warp_claim(P, rcp, &u)) break;
     const Unit U = P.units[u];
-    const uint32_t hs = P.bstart[U.h], he = P.bstart[U.h + 1];
+    const UnitView V = unit_view(P, u);
+    const float4* X = (const float4*)V.xs;
+    const uint32_t hs = V.bstart[U.h], he = V.bstart[U.h + 1];
     const uint32_t a0 = hs + U.chunk * CH;
     const uint32_t na = min((uint32_t)CH, he - a0);
     __syncwarp();
@@ -238,7 +327,7 @@ k_join_f32(const JoinParams P) {
     __syncwarp();
     uint32_t s = U.s0, off = 0;
     while (s < U.s1) {
-      const CandTile t = next_tile(P, s, off, U.s1);
+      const CandTile t = next_tile(V.nbr, V.bstart, s, off, U.s1);
       const uint32_t q = t.q;
       const float4* qrow = X + (size_t)(t.qv ? q : a0) * nq4;
       float acc[CH];
@@ -247,7 +336,7 @@ k_join_f32(const JoinParams P) {
 #pragma unroll
       for (int a = 0; a < CH; ++a) {
         if (a >= (int)na) break;
-        m |= (acc[a] <= P.t_hi ? 1u : 0u) << a;
+        m |= (acc[a] <= V.t_hi ? 1u : 0u) << a;
       }
       m = t.qv ? (m & home_mask(na, q >= hs && q < he, q, a0, CH)) : 0u;
       if (__any_sync(FULL_MASK, m != 0)) {
@@ -255,18 +344,18 @@ k_join_f32(const JoinParams P) {
 #pragma unroll
         for (int a = 0; a < CH; ++a) {
           if (a >= (int)na) break;
-          lo_m |= (acc[a] <= P.t_lo ? 1u : 0u) << a;
+          lo_m |= (acc[a] <= V.t_lo ? 1u : 0u) << a;
         }
         lo_m &= m;
         const uint32_t band = m & ~lo_m;
-        stage_hits(ps, P, lo_m, a0, q, &P.ctr->pairs, P.pairs, P.cap);
+        stage_hits(ps, V.ids, lo_m, a0, q, &P.ctr->pairs, P.pairs, P.cap, P.inst_pairs, V.inst, rcp);
         if (__any_sync(FULL_MASK, band != 0u))  // decided later, all at once (k_band_check)
-          stage_hits(bs, P, band, a0, q, &P.ctr->band_n, P.band_list, P.band_cap);
+          stage_hits(bs, V.ids, band, a0, q, &P.ctr->band_n, P.band_list, P.band_cap, nullptr, V.inst, rcb);
       }
     }
   }
-  stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
-  stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap);
+  stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap, P.inst_pairs, rcp);
+  stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap, nullptr, rcb);
 }
 
 // FP32 filter for d <= 32: the lane's candidate row lives in registers as DQ
@@ -283,14 +372,16 @@ k_join_f32r(const JoinParams P) {
   unsigned long long* stg = reinterpret_cast<unsigned long long*>(smem_f4r + (size_t)(blockDim.x >> 5) * CH * DQ);
   PairStage ps{stg + (size_t)w * PSTAGE, 0};
   PairStage bs{stg + (size_t)((blockDim.x >> 5) + w) * PSTAGE, 0};
-  const float4* X = (const float4*)P.xs;
+  const RingPair RP = ring_ctx(P);
+  const RingCtx* rcp = P.ring ? &RP.pairs : nullptr;
+  const RingCtx* rcb = P.ring ? &RP.band : nullptr;
   for (;;) {
     unsigned long long u = 0;
-    if (lane == 0) u = atomicAdd(&P.ctr->next_unit, 1ull);
-    u = __shfl_sync(FULL_MASK, u, 0);
-    if (u >= P.n_units) break;
+    if (!warp_claim(P, rcp, &u)) break;
     const Unit U = P.units[u];
-    const uint32_t hs = P.bstart[U.h], he = P.bstart[U.h + 1];
+    const UnitView V = unit_view(P, u);
+    const float4* X = (const float4*)V.xs;
+    const uint32_t hs = V.bstart[U.h], he = V.bstart[U.h + 1];
     const uint32_t a0 = hs + U.chunk * CH;
     const uint32_t na = min((uint32_t)CH, he - a0);
     __syncwarp();
@@ -299,7 +390,7 @@ k_join_f32r(const JoinParams P) {
     __syncwarp();
     uint32_t s = U.s0, off = 0;
     while (s < U.s1) {
-      const CandTile t = next_tile(P, s, off, U.s1);
+      const CandTile t = next_tile(V.nbr, V.bstart, s, off, U.s1);
       const uint32_t q = t.q;
       const ulonglong2* qrow = reinterpret_cast<const ulonglong2*>(X + (size_t)(t.qv ? q : a0) * DQ);
       ulonglong2 qq[DQ];  // the candidate row as pairs of floats
@@ -333,22 +424,22 @@ k_join_f32r(const JoinParams P) {
           float lo, hi;
           asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(acc2[i]));
           const float acc = lo + hi;
-          m |= (acc <= P.t_hi ? 1u : 0u) << (g * 8 + i);
-          lo_m |= (acc <= P.t_lo ? 1u : 0u) << (g * 8 + i);
+          m |= (acc <= V.t_hi ? 1u : 0u) << (g * 8 + i);
+          lo_m |= (acc <= V.t_lo ? 1u : 0u) << (g * 8 + i);
         }
       }
       m = t.qv ? (m & home_mask(na, q >= hs && q < he, q, a0, CH)) : 0u;
       if (__any_sync(FULL_MASK, m != 0)) {
         lo_m &= m;
         const uint32_t band = m & ~lo_m;
-        stage_hits(ps, P, lo_m, a0, q, &P.ctr->pairs, P.pairs, P.cap);
+        stage_hits(ps, V.ids, lo_m, a0, q, &P.ctr->pairs, P.pairs, P.cap, P.inst_pairs, V.inst, rcp);
         if (__any_sync(FULL_MASK, band != 0u))  // decided later, all at once (k_band_check)
-          stage_hits(bs, P, band, a0, q, &P.ctr->band_n, P.band_list, P.band_cap);
+          stage_hits(bs, V.ids, band, a0, q, &P.ctr->band_n, P.band_list, P.band_cap, nullptr, V.inst, rcb);
       }
     }
   }
-  stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
-  stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap);
+  stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap, P.inst_pairs, rcp);
+  stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap, nullptr, rcb);
 }
 
 // ---------------------------------------------------------------- FP64 plain
@@ -391,16 +482,18 @@ k_join_f64(const JoinParams P) {
   const uint32_t nq2 = P.dpad >> 1;
   double2* sA = smem_d2 + (size_t)w * CH * nq2;
   PairStage ps{reinterpret_cast<unsigned long long*>(smem_d2 + (size_t)(blockDim.x >> 5) * CH * nq2) + (size_t)w * PSTAGE, 0};
-  const double2* X = (const double2*)P.xs;
-  const double thr = P.eps2 + P.amb;
   uint32_t amb_cnt = 0;
+  const RingPair RP = ring_ctx(P);
+  const RingCtx* rcp = P.ring ? &RP.pairs : nullptr;
+  const RingCtx* rcb = P.ring ? &RP.band : nullptr;
   for (;;) {
     unsigned long long u = 0;
-    if (lane == 0) u = atomicAdd(&P.ctr->next_unit, 1ull);
-    u = __shfl_sync(FULL_MASK, u, 0);
-    if (u >= P.n_units) break;
+    if (!warp_claim(P, rcp, &u)) break;
     const Unit U = P.units[u];
-    const uint32_t hs = P.bstart[U.h], he = P.bstart[U.h + 1];
+    const UnitView V = unit_view(P, u);
+    const double2* X = (const double2*)V.xs;
+    const double thr = V.eps2 + V.amb;
+    const uint32_t hs = V.bstart[U.h], he = V.bstart[U.h + 1];
     const uint32_t a0 = hs + U.chunk * CH;
     const uint32_t na = min((uint32_t)CH, he - a0);
     __syncwarp();
@@ -409,7 +502,7 @@ k_join_f64(const JoinParams P) {
     __syncwarp();
     uint32_t s = U.s0, off = 0;
     while (s < U.s1) {
-      const CandTile t = next_tile(P, s, off, U.s1);
+      const CandTile t = next_tile(V.nbr, V.bstart, s, off, U.s1);
       const uint32_t q = t.q;
       const double2* qrow = X + (size_t)(t.qv ? q : a0) * nq2;
       double acc[CH];
@@ -425,16 +518,16 @@ k_join_f64(const JoinParams P) {
         uint32_t acc_m = 0, amb_m = 0;
 #pragma unroll
         for (int a = 0; a < CH; ++a) {
-          acc_m |= (acc[a] <= P.eps2 ? 1u : 0u) << a;
-          amb_m |= (fabs(acc[a] - P.eps2) <= P.amb ? 1u : 0u) << a;
+          acc_m |= (acc[a] <= V.eps2 ? 1u : 0u) << a;
+          amb_m |= (fabs(acc[a] - V.eps2) <= V.amb ? 1u : 0u) << a;
         }
         acc_m &= m;
         amb_cnt += __popc(amb_m & m);
-        stage_hits(ps, P, acc_m, a0, q, &P.ctr->pairs, P.pairs, P.cap);
+        stage_hits(ps, V.ids, acc_m, a0, q, &P.ctr->pairs, P.pairs, P.cap, P.inst_pairs, V.inst, rcp);
       }
     }
   }
-  stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
+  stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap, P.inst_pairs, rcp);
   add_counter(&P.ctr->ambiguous, amb_cnt);
 }
 
@@ -445,21 +538,71 @@ k_join_f64(const JoinParams P) {
 // FP64 predicate, one pair per thread, and appends the accepted ones (same
 // packing) to the pair list.  The list length is read on the device.
 __global__ void __launch_bounds__(256) k_band_check(const JoinParams P) {
-  const unsigned long long n = min(*(volatile unsigned long long*)&P.ctr->band_n, P.band_cap);
+  // ring mode: the slice [band0, band1) of the band list, entries of deferred
+  // units skipped, accepted pairs written with their unit's tag (the slice
+  // is sized to fit the ring); otherwise the whole list
+  const unsigned long long n =
+      P.ring ? P.band1 : min(*(volatile unsigned long long*)&P.ctr->band_n, P.band_cap);
   const int lane = threadIdx.x & 31;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   uint32_t cnt = 0, amb = 0;
-  for (unsigned long long i0 = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < n;
-       i0 += stride) {
+  for (unsigned long long i0 = (P.ring ? P.band0 : 0) + (unsigned long long)blockIdx.x * blockDim.x +
+                               (threadIdx.x & ~31u);
+       i0 < n; i0 += stride) {
     const unsigned long long i = i0 + lane;
     bool acc = false;
     unsigned long long e = 0;
-    if (i < n) {
+    uint32_t tag = 0;
+    if (i < n && P.ring) {
+      tag = P.band_tags[i];
+      if (P.deferred[tag]) e = ~0ull;  // that unit runs again: its band entries come again
+    }
+    if (i < n && e != ~0ull) {
       e = P.band_list[i];
-      const double sd = exact_sqdist(P, (uint32_t)(e >> 32), (uint32_t)e);
+      const uint32_t gi = (uint32_t)(e >> 32), gj = (uint32_t)e;
+      double sd, eps2 = P.eps2, ambv = P.amb;
+      if (P.insts) {  // the pair's instance: the last one whose first global row is <= gi
+        uint32_t lo = 0, hi = P.n_inst - 1;
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi + 1) >> 1;
+          if (P.inst_row0[mid] <= gi) lo = mid; else hi = mid - 1;
+        }
+        const InstDesc& I = P.insts[lo];
+        sd = exact_sqdist(I.raw, I.raw_f32, I.d, gi - I.row0, gj - I.row0);
+        eps2 = I.eps2;
+        ambv = I.amb;
+        if (sd <= eps2) atomicAdd(&P.inst_pairs[lo], 1ull);
+      } else if (P.inv) {
+        // the FP32 filter first (its bound is ~2^-24 relative where the
+        // tensor cores' is ~2^-16 or wider): only its own, much narrower,
+        // band goes on to the FP64 predicate
+        const float4* a = reinterpret_cast<const float4*>(P.xf32 + (size_t)P.inv[gi] * P.dpad32);
+        const float4* b = reinterpret_cast<const float4*>(P.xf32 + (size_t)P.inv[gj] * P.dpad32);
+        float s0 = 0.f, s1 = 0.f;
+        for (uint32_t c = 0; c < P.dpad32 / 4; ++c) {
+          const float4 x = a[c], y = b[c];
+          float t = x.x - y.x;
+          s0 = fmaf(t, t, s0);
+          t = x.y - y.y;
+          s1 = fmaf(t, t, s1);
+          t = x.z - y.z;
+          s0 = fmaf(t, t, s0);
+          t = x.w - y.w;
+          s1 = fmaf(t, t, s1);
+        }
+        const float s32 = s0 + s1;
+        if (s32 <= P.t_lo)
+          sd = -1.0;  // accepted
+        else if (s32 > P.t_hi)
+          sd = INFINITY;  // rejected
+        else
+          sd = exact_sqdist(P.raw, P.raw_f32, P.d, gi, gj);
+      } else {
+        sd = exact_sqdist(P.raw, P.raw_f32, P.d, gi, gj);
+      }
       ++cnt;
-      if (fabs(sd - P.eps2) <= P.amb) ++amb;
-      acc = sd <= P.eps2;
+      if (fabs(sd - eps2) <= ambv) ++amb;
+      acc = sd <= eps2;
     }
     const uint32_t m = __ballot_sync(FULL_MASK, acc);
     if (m) {
@@ -468,7 +611,10 @@ __global__ void __launch_bounds__(256) k_band_check(const JoinParams P) {
       base = __shfl_sync(FULL_MASK, base, 0);
       if (acc && P.pairs) {
         const unsigned long long pos = base + __popc(m & ((1u << lane) - 1u));
-        if (pos < P.cap) P.pairs[pos] = e;
+        if (pos < P.cap) {
+          P.pairs[pos] = e;
+          if (P.ring) P.pair_tags[pos] = tag;
+        }
       }
     }
   }
@@ -507,8 +653,8 @@ static void launch_persistent(mistic_handle_s* h, K kern, size_t smem_per_warp, 
   MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));
   if (per_sm < 1) throw Error(MISTIC_ERR_TOO_LARGE, "join kernel does not fit on an SM for this dimensionality");
   const unsigned long long want = (P.n_units + warps - 1) / warps;
-  const unsigned grid =
-      (unsigned)std::min<unsigned long long>((unsigned long long)per_sm * h->sms, want ? want : 1);
+  unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)per_sm * h->sms, want ? want : 1);
+  if (P.grid_cap) grid = std::min(grid, P.grid_cap);
   if (getenv("MISTIC_DEBUG"))
     fprintf(stderr, "[mistic] %s warps=%d smem=%zu occupancy=%d grid=%u units=%llu\n", name, warps, smem, per_sm, grid,
             (unsigned long long)P.n_units);

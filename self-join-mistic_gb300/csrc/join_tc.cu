@@ -88,6 +88,7 @@ constexpr uint32_t FLAG_FIRST = 1, FLAG_LAST = 2, FLAG_END = 4;
 struct TileMeta {
   uint32_t a0, na, ncols, flags, ng;  // ng: 128-row MMA tiles of this unit (1..G)
   uint32_t hcr, hq;  // columns [hcr & 255, hcr >> 8) hold home-bin rows, the first at sorted position hq
+  uint32_t inst;     // instance of the unit (fused batch joins; else 0)
 };
 
 template <int NS, int G, int RAW>
@@ -245,7 +246,6 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
   __nv_bfloat16* Raw = Blo + NS * OPB;  // RAW landing slots (raw FP32 rows in the chunk layout, 2 * OPB each)
   unsigned long long* pstage = reinterpret_cast<unsigned long long*>(Raw + RAW * 2 * OPB);  // 2 NEPI x PSTAGE
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const float* X = (const float*)P.xs;
   volatile uint32_t* abort_flag = &S.abort_flag;
 
   if (tid == 0) {
@@ -304,9 +304,17 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
       const long long cu0 = T.prof ? clock64() : 0;
       const uint32_t slot = pf++ & 1;
       if (tid == 0) {
-        const unsigned long long uu = atomicAdd(&T.ctr->next_unit, 1ull);
+        // claim index -> unit: units deferred by the last ring pass first,
+        // then the list from main_start (the identity outside ring mode)
+        const unsigned long long t = atomicAdd(&T.ctr->next_unit, 1ull);
+        const unsigned long long uu = t < T.n_def_in ? (unsigned long long)T.def_in[t] : T.main_start + (t - T.n_def_in);
         S.unit = uu;
         bool go = uu < T.n_units && !*abort_flag;
+        if (go && P.ring && *(volatile unsigned long long*)&P.ctr->stop) {  // the ring filled: leave it for the next pass
+          const RingCtx rc{P.pair_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
+          ring_defer(&rc, P.tag_base_tc + (uint32_t)uu);
+          go = false;
+        }
         if (go && unit_k > 0) go = wait_or_abort(&S.afree, (unit_k - 1) & 1, abort_flag, T.wait_limit);  // A no longer read
         S.pflag[slot] = go ? 1u : 0u;
       }
@@ -317,7 +325,23 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
       }
       const unsigned long long u = S.unit;
       const Unit U = T.units[u];
-      const uint32_t hs = P.bstart[U.h], he = P.bstart[U.h + 1];
+      // the unit's instance: its arrays and bound constants (fused batch
+      // joins), or the launch's own
+      const float* X = (const float*)P.xs;
+      const uint32_t *bstart = P.bstart, *nbr = P.nbr, *ids = P.ids;
+      TcBound tb = T.b;
+      uint32_t inst = 0;
+      if (T.unit_inst) {
+        inst = T.unit_inst[u];
+        const InstDesc& I = P.insts[inst];
+        X = (const float*)I.xs;
+        bstart = I.bstart;
+        nbr = I.nbr;
+        ids = I.ids;
+        tb = I.tcb;
+      }
+      if (P.ring) inst = P.tag_base_tc + (uint32_t)u;  // the ring's tag of this unit's pairs
+      const uint32_t hs = bstart[U.h], he = bstart[U.h + 1];
       const uint32_t a0 = hs + U.chunk * (TM * G);
       const uint32_t na = min((uint32_t)(TM * G), he - a0);
       const uint32_t ng = (na + TM - 1) / TM;
@@ -332,7 +356,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
 #pragma unroll
       for (int i = 0; i < (G + 1) / 2; ++i) {
         const uint32_t r = (2 * i + half) * TM + prow;
-        my_aid[i] = (2 * i + (int)half < G && r < na) ? P.ids[a0 + r] : 0u;
+        my_aid[i] = (2 * i + (int)half < G && r < na) ? ids[a0 + r] : 0u;
       }
       {
         for (uint32_t g = 0; g < ng; ++g) {
@@ -372,9 +396,9 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
           const uint32_t nb = min((uint32_t)WIN, U.s1 - seg_next);
           uint32_t st0 = 0, sz0 = 0, bn = 0xffffffffu;
           if ((uint32_t)tid < nb) {
-            bn = P.nbr[seg_next + tid];
-            st0 = P.bstart[bn];
-            sz0 = P.bstart[bn + 1] - st0;
+            bn = nbr[seg_next + tid];
+            st0 = bstart[bn];
+            sz0 = bstart[bn + 1] - st0;
           }
           const uint32_t incl = warp_scan_incl(sz0);
           if (lane == 31) S.scan_ws[warp] = incl;
@@ -438,7 +462,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         }
         if (prow < ncols) {
           if (half == 0)
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(&iddst[prow])), "l"(P.ids + q)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(&iddst[prow])), "l"(ids + q)
                          : "memory");
           load_half<KP>(dh, dl, prow, half, X + (size_t)q * P.dpad, P.dpad);
         }
@@ -512,7 +536,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         const float part = conv_pass1<KP>(sh, sl, bh, bl, prow, half, ok, S.cadd_b, -2.f, P.d);
         const float nq2 = (part + __shfl_xor_sync(FULL_MASK, part, 16)) * 0.25f;
         float tcol = 0.f, dl = 0.f;
-        if (ok && !column_threshold(T, ra2max, nq2, &tcol, &dl)) {
+        if (ok && !column_threshold(tb, ra2max, nq2, &tcol, &dl)) {
           tcol = 1e30f;   // every row of this column becomes a candidate ...
           dl = INFINITY;  // ... and none is accepted without the FP64 check
         }
@@ -529,7 +553,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
           if (2 * i + (int)half < G) S.aid[st][(2 * i + half) * TM + prow] = my_aid[i];
         if (tid == 0) {
           S.meta[st] = TileMeta{a0, na, ncols, (first ? FLAG_FIRST : 0u) | (last ? FLAG_LAST : 0u), ng,
-                                S.hx[tile & 3][0], S.hx[tile & 3][1]};
+                                S.hx[tile & 3][0], S.hx[tile & 3][1], inst};
           n_tiles += 1;
           n_cells += (unsigned long long)na * ncols;
         }
@@ -665,6 +689,10 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
     const uint32_t cblk0 = (warp - EPI0) >> 2;
     PairStage ps{pstage + (warp - EPI0) * PSTAGE, 0};
     PairStage bs{pstage + (NEPI + warp - EPI0) * PSTAGE, 0};
+    const RingCtx rcp_{P.pair_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
+    const RingCtx rcb_{P.band_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
+    const RingCtx* rcp = P.ring ? &rcp_ : nullptr;
+    const RingCtx* rcb = P.ring ? &rcb_ : nullptr;
     uint32_t tile = 0, mt = 0, g = 0;
     long long ew_dfull = 0, ec_ld = 0, ec_slow = 0, ec_stage = 0;
     const long long e_start = T.prof ? clock64() : 0;
@@ -737,7 +765,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         if (T.prof) ec_slow += cs1 - cs0;
         const uint32_t ia = (acc_bits | band_bits) ? S.aid[st][row] : 0u;
         auto emit = [&](PairStage& stg, uint32_t bits, unsigned long long* counter, unsigned long long* list,
-                        unsigned long long lcap) {
+                        unsigned long long lcap, unsigned long long* ip, const RingCtx* rc) {
           stage_pairs(
               stg, __popc(bits),
               [&](uint32_t) {
@@ -747,10 +775,12 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
                 const uint32_t lo = ia < iq ? ia : iq, hi = ia < iq ? iq : ia;
                 return ((unsigned long long)lo << 32) | hi;
               },
-              counter, list, lcap);
+              counter, list, lcap, ip, M.inst, rc);
         };
-        if (__any_sync(FULL_MASK, acc_bits != 0u)) emit(ps, acc_bits, &P.ctr->pairs, P.pairs, P.cap);
-        if (__any_sync(FULL_MASK, band_bits != 0u)) emit(bs, band_bits, &P.ctr->band_n, P.band_list, P.band_cap);
+        if (__any_sync(FULL_MASK, acc_bits != 0u))
+          emit(ps, acc_bits, &P.ctr->pairs, P.pairs, P.cap, P.inst_pairs, rcp);
+        if (__any_sync(FULL_MASK, band_bits != 0u))
+          emit(bs, band_bits, &P.ctr->band_n, P.band_list, P.band_cap, nullptr, rcb);
         if (T.prof) ec_stage += clock64() - cs1;
       }
       }
@@ -769,8 +799,8 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         ++g;
       }
     }
-    stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
-    stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap);
+    stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap, P.inst_pairs, rcp);
+    stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap, nullptr, rcb);
     if (T.prof && lane == 0) {
       atomicAdd(&T.ctr->prof[5], (unsigned long long)ew_dfull);
       atomicAdd(&T.ctr->prof[6], (unsigned long long)(clock64() - e_start));
@@ -809,7 +839,8 @@ void launch_tc(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
   int per_sm = 0;
   MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join_tc<KP, NS, G, RAW, NEPI>, NT, dyn));
   if (per_sm < 1) throw Error(MISTIC_ERR_TOO_LARGE, "tensor-core join does not fit on an SM");
-  const unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)h->sms, T.n_units);
+  unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)h->sms, T.n_units);
+  if (T.grid_cap) grid = std::min(grid, T.grid_cap);
   if (getenv("MISTIC_DEBUG"))
     fprintf(stderr, "[mistic] join_tc KP=%d NS=%d G=%d RAW=%d NEPI=%d dyn=%zu occupancy=%d grid=%u units=%llu\n", KP,
             NS, G, RAW, NEPI, dyn, per_sm, grid, (unsigned long long)T.n_units);

@@ -108,6 +108,7 @@ struct __align__(16) WGroup {
   float na[WG * WM];     // |a|^2 of the home rows
   uint32_t a0, nrows, ncols, ng, flags;
   uint32_t hlo, hhi, hq0;  // columns [hlo, hhi) are home-bin rows, column hlo at sorted position hq0
+  uint32_t tag;            // the pair ring's tag of the group's unit (0 outside ring mode)
 };
 
 struct WShared {
@@ -352,10 +353,19 @@ __global__ void __launch_bounds__(WTHREADS, 1)
     for (;;) {
       const uint32_t slot = pf++ & 1;
       if (tid == 0) {
-        const unsigned long long uu = atomicAdd(&T.ctr->next_unit, 1ull);
+        // claim index -> unit: units deferred by the last ring pass first,
+        // then the list from main_start (the identity outside ring mode)
+        const unsigned long long t = atomicAdd(&T.ctr->next_unit, 1ull);
+        const unsigned long long uu = t < T.n_def_in ? (unsigned long long)T.def_in[t] : T.main_start + (t - T.n_def_in);
         S.unit = uu;
         S.ra2max = 0;
-        S.pflag[slot] = (uu < T.n_units && !*abort_flag) ? 1u : 0u;
+        bool go = uu < T.n_units && !*abort_flag;
+        if (go && P.ring && *(volatile unsigned long long*)&P.ctr->stop) {  // the ring filled: leave it for the next pass
+          const RingCtx rc{P.pair_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
+          ring_defer(&rc, P.tag_base_tc + (uint32_t)uu);
+          go = false;
+        }
+        S.pflag[slot] = go ? 1u : 0u;
       }
       wprod_sync();
       if (!S.pflag[slot]) break;
@@ -431,7 +441,7 @@ __global__ void __launch_bounds__(WTHREADS, 1)
           qid = P.ids[q];
           const float nq2 = T.xn[q];
           float tcol;
-          if (column_threshold(T, ra2max, nq2, &tcol, &dl)) {
+          if (column_threshold(T.b, ra2max, nq2, &tcol, &dl)) {
             hqv = nq2 - tcol;
           } else {
             hqv = -1e30f;   // every row of this column becomes a candidate ...
@@ -468,6 +478,7 @@ __global__ void __launch_bounds__(WTHREADS, 1)
           Gm.hlo = hlo;
           Gm.hhi = hhi;
           Gm.hq0 = hq0;
+          Gm.tag = P.ring ? P.tag_base_tc + (uint32_t)S.unit : 0u;
           n_tiles += (unsigned long long)ng * ((ncols + 127) / 128);
           n_cells += (unsigned long long)nrows * ncols;
         }
@@ -706,6 +717,10 @@ __global__ void __launch_bounds__(WTHREADS, 1)
     const uint32_t cblk0 = (warp - WEPI0) >> 2;
     PairStage ps{pstage + (warp - WEPI0) * PSTAGE, 0};
     PairStage bs{pstage + (WNEPI + warp - WEPI0) * PSTAGE, 0};
+    const RingCtx rcp_{P.pair_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
+    const RingCtx rcb_{P.band_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
+    const RingCtx* rcp = P.ring ? &rcp_ : nullptr;
+    const RingCtx* rcb = P.ring ? &rcb_ : nullptr;
     uint32_t group = 0;
     uint32_t use[WG] = {0, 0};
     bool run = true;
@@ -776,7 +791,7 @@ __global__ void __launch_bounds__(WTHREADS, 1)
             __syncwarp();
             const uint32_t ia = (acc_bits | band_bits) ? Gm.aid[row] : 0u;
             auto emit = [&](PairStage& stg, uint32_t bits, unsigned long long* counter, unsigned long long* list,
-                            unsigned long long lcap) {
+                            unsigned long long lcap, const RingCtx* rc) {
               stage_pairs(
                   stg, __popc(bits),
                   [&](uint32_t) {
@@ -786,10 +801,11 @@ __global__ void __launch_bounds__(WTHREADS, 1)
                     const uint32_t lo = ia < iq ? ia : iq, hi = ia < iq ? iq : ia;
                     return ((unsigned long long)lo << 32) | hi;
                   },
-                  counter, list, lcap);
+                  counter, list, lcap, nullptr, Gm.tag, rc);
             };
-            if (__any_sync(FULL_MASK, acc_bits != 0u)) emit(ps, acc_bits, &P.ctr->pairs, P.pairs, P.cap);
-            if (__any_sync(FULL_MASK, band_bits != 0u)) emit(bs, band_bits, &P.ctr->band_n, P.band_list, P.band_cap);
+            if (__any_sync(FULL_MASK, acc_bits != 0u)) emit(ps, acc_bits, &P.ctr->pairs, P.pairs, P.cap, rcp);
+            if (__any_sync(FULL_MASK, band_bits != 0u))
+              emit(bs, band_bits, &P.ctr->band_n, P.band_list, P.band_cap, rcb);
           }
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
@@ -801,8 +817,8 @@ __global__ void __launch_bounds__(WTHREADS, 1)
       if (lane == 0) mbar_arrive(&S.gfree[gs]);
       ++group;
     }
-    stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap);
-    stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap);
+    stage_flush(ps, &P.ctr->pairs, P.pairs, P.cap, nullptr, rcp);
+    stage_flush(bs, &P.ctr->band_n, P.band_list, P.band_cap, nullptr, rcb);
     if (T.prof && lane == 0) {
       atomicAdd(&T.ctr->prof[5], (unsigned long long)ew);
       atomicAdd(&T.ctr->prof[6], (unsigned long long)(clock64() - e_start));
@@ -884,7 +900,8 @@ void launch_tcw(mistic_handle_s* h, const JoinParams& P, const TcParams& T) {
   int per_sm = 0;
   MCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_join_tcw<PREC>, WTHREADS, dyn));
   if (per_sm < 1) throw Error(MISTIC_ERR_TOO_LARGE, "long-row tensor-core join does not fit on an SM");
-  const unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)h->sms, T.n_units);
+  unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)h->sms, T.n_units);
+  if (T.grid_cap) grid = std::min(grid, T.grid_cap);
   if (getenv("MISTIC_DEBUG"))
     fprintf(stderr, "[mistic] join_tcw PREC=%d KD=%u dyn=%zu occupancy=%d grid=%u units=%llu\n", PREC, T.kd, dyn,
             per_sm, grid, (unsigned long long)T.n_units);

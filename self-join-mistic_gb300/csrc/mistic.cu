@@ -459,7 +459,10 @@ TuneCache& tune_cache() {
   return *c;
 }
 
-using TuneMeasure = std::function<void(const TuneCandidate&, uint32_t sample, double* ms, unsigned long long* cands)>;
+// times one candidate on the home-point sample 1/sample; reports the sample's
+// candidate pairs and work units
+using TuneMeasure = std::function<void(const TuneCandidate&, uint32_t sample, double* ms, unsigned long long* cands,
+                                       unsigned long long* units)>;
 
 // Looks the shape up, or times the candidates on a sample and records the
 // fastest.  Returns false when tuning is off (the defaults then stand).
@@ -491,7 +494,7 @@ bool tune_lookup(mistic_handle_s* h, const mistic_opts& o, uint32_t d, mistic_dt
   }
   const int eps_cls = (eps2 > 0 && R > 0) ? (int)std::floor(std::log2(R * R / eps2)) : 0;
   char key[160];
-  snprintf(key, sizeof key, "v1 d=%u dt=%d %s bins=%d,%d r2e=%d", d, (int)dt, wide ? "tcw" : "tc", c50, c90, eps_cls);
+  snprintf(key, sizeof key, "v2 d=%u dt=%d %s bins=%d,%d r2e=%d", d, (int)dt, wide ? "tcw" : "tc", c50, c90, eps_cls);
   if (tune_cache().find(key, out)) return true;
   // candidates
   std::vector<TuneCandidate> cands;
@@ -499,23 +502,31 @@ bool tune_lookup(mistic_handle_s* h, const mistic_opts& o, uint32_t d, mistic_dt
     std::vector<int> precs = {0};
     if (prec_default == 1) precs.push_back(1);  // single bf16 only where its bound fits the cap
     for (int pr : precs)
-      for (uint32_t t : {4u, 8u, 16u}) cands.push_back({t, pr});
+      for (uint32_t t : {1u, 8u}) cands.push_back({t, pr});
   } else {
     const uint32_t t0 = tc_min_bin(d, false);
     for (uint32_t t : {std::max(1u, t0 / 2), t0, std::min(512u, 2 * t0)})
       if (cands.empty() || cands.back().tc_min != t) cands.push_back({t, 0});
   }
-  // sample: about 1/64 of the home points; grown when one run takes long
+  // sample: about 1/64 of the home points, but enough work units that the
+  // persistent grid is not timed on its tail (units of long rows are few and
+  // large: at least ~20 a CTA), and no more than a few hundred ms a run
   uint32_t S = 64;
   double best = 1e300;
   Tuned bt{cands[0].tc_min, cands[0].prec};
+  const unsigned long long want_units = 20ull * (unsigned long long)h->sms;
   for (size_t i = 0; i < cands.size(); ++i) {
     double ms = 0;
-    unsigned long long cc = 0;
-    measure(cands[i], S, &ms, &cc);
-    if (i == 0 && ms > 150.0) {  // keep the tuning pass short: re-time on a smaller sample
-      S = (uint32_t)std::min(4096.0, S * ms / 100.0);
-      measure(cands[i], S, &ms, &cc);
+    unsigned long long cc = 0, uu = 0;
+    measure(cands[i], S, &ms, &cc, &uu);
+    if (i == 0) {
+      uint32_t S2 = S;
+      if (uu < want_units) S2 = (uint32_t)std::max(1.0, S * (double)uu / (double)want_units);
+      if (ms * S / S2 > 400.0) S2 = (uint32_t)std::min(4096.0, std::ceil(S * ms / 400.0));
+      if (S2 != S) {
+        S = S2;
+        measure(cands[i], S, &ms, &cc, &uu);
+      }
     }
     if (getenv("MISTIC_DEBUG"))
       fprintf(stderr, "[mistic] tune %s: tc_min=%u prec=%d sample 1/%u: %.3f ms (%llu candidates)\n", key,
@@ -532,8 +543,67 @@ bool tune_lookup(mistic_handle_s* h, const mistic_opts& o, uint32_t d, mistic_dt
 
 // ------------------------------------------------------------------ the pipeline
 
+// Phase one of a fused batch join (mistic_batch_selfjoin): run_selfjoin
+// builds the instance's index and work lists, and then -- when the instance
+// joins on the FP32 filter and/or the short-row tensor-core kernel --
+// copies them into device memory obtained from `alloc` and describes them
+// here instead of joining.  Ids are shifted by row0 so that pairs of
+// different instances stay apart.  Instances that need the plain FP64 join
+// or the K-chunked kernel are joined in full as usual (exported = false).
+struct BatchExport {
+  uint32_t row0 = 0;
+  std::function<void*(size_t)> alloc;  // device bytes (256-byte aligned), or null when the batch arena is full
+  bool exported = false;
+  InstDesc desc{};
+  uint32_t dpad32 = 0;
+  const Unit* units = nullptr;     // CUDA-core units, in the allocated memory
+  uint32_t n_units = 0;
+  const Unit* units_tc = nullptr;  // tensor-core units
+  uint32_t n_units_tc = 0;
+  int CH = 0;                      // CUDA-core chunk
+};
+
+// Pair ring drain: the entries [0, m) that hold a pair of a unit not
+// deferred in this pass, compacted into out (one atomic per warp).
+__global__ void k_ring_drain(const unsigned long long* __restrict__ ring, const uint32_t* __restrict__ tags,
+                             const uint32_t* __restrict__ deferred, unsigned long long m,
+                             unsigned long long* __restrict__ out, unsigned long long* __restrict__ out_n) {
+  const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool keep = false;
+  unsigned long long v = 0;
+  if (i < m) {
+    const uint32_t t = tags[i];
+    keep = t != 0xffffffffu && !deferred[t];
+    if (keep) v = ring[i];
+  }
+  const uint32_t b = __ballot_sync(0xffffffffu, keep);
+  if (!b) return;
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(out_n, (unsigned long long)__popc(b));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (keep) out[base + __popc(b & ((1u << lane) - 1u))] = v;
+}
+
+// Clears the deferred flags of the tags in list[0 .. n).
+__global__ void k_clear_flags(uint32_t* __restrict__ flags, const uint32_t* __restrict__ list, unsigned long long n) {
+  const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flags[list[i]] = 0u;
+}
+
+// inv[ids[p]] = p: sorted position of every original row id.
+__global__ void k_inverse_perm(const uint32_t* __restrict__ ids, size_t n, uint32_t* __restrict__ inv) {
+  const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n) inv[ids[p]] = (uint32_t)p;
+}
+
+__global__ void k_add_u32(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, size_t n, uint32_t add) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i] + add;
+}
+
 void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mistic_dtype dt, uint32_t k,
-                  double eps, const mistic_opts* opts_in, mistic_result* r) {
+                  double eps, const mistic_opts* opts_in, mistic_result* r, BatchExport* ex = nullptr) {
   const auto wall0 = std::chrono::steady_clock::now();
   mistic_opts o;
   mistic_opts_init(&o);
@@ -837,6 +907,14 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   jp.amb = 4.0 * (nextafter(eps2, INFINITY) - eps2);
   JoinCounters* ctr = abuf<JoinCounters>(h, "ctr", 2);  // [0] CUDA-core join, [1] tensor-core cursor
   jp.ctr = ctr;
+  if (!fp64) {  // band pairs are pre-decided with the FP32 filter on the sorted FP32 rows
+    uint32_t* inv = abuf<uint32_t>(h, "inv", n);
+    k_inverse_perm<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(ids, n, inv);
+    launched(h, "inverse_perm");
+    jp.inv = inv;
+    jp.xf32 = xf;
+    jp.dpad32 = dpad32;
+  }
   TcParams tp{};
   int prepared = -1;  // operand precision the K-chunked kernel's rows are prepared at
   // tensor-core parameters at operand precision pr (rows prepared on demand)
@@ -846,17 +924,17 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     const double gd = d * u / (1.0 - d * u);
     const double g64 = (d + 2) * ldexp(1.0, -53) * 1.01;
     tp.ctr = ctr + 1;
-    tp.eps2_lo = (float)(eps2 / (1.0 + g64));
-    if ((double)tp.eps2_lo > eps2 / (1.0 + g64)) tp.eps2_lo = nextafterf(tp.eps2_lo, 0.f);
-    tp.eps2_hi = (float)(eps2 / (1.0 - g64));
-    if ((double)tp.eps2_hi < eps2 / (1.0 - g64)) tp.eps2_hi = nextafterf(tp.eps2_hi, INFINITY);
-    tp.kappa = (float)tc_kappa(d, wide, pr);
-    tp.ginf = (float)(1.0 / (1.0 - gd) * (1.0 + 1e-6));
-    tp.uR2 = (float)(2.0 * u * R * 1.0001);
-    tp.u1 = (float)(u * (1.0 + u) * 1.0001);
-    tp.Dp = (float)(1.1 * sqrt(eps2));
-    tp.cap = (float)(0.1 * eps2);
-    tp.margin = (float)(1e-6 * eps2);
+    tp.b.eps2_lo = (float)(eps2 / (1.0 + g64));
+    if ((double)tp.b.eps2_lo > eps2 / (1.0 + g64)) tp.b.eps2_lo = nextafterf(tp.b.eps2_lo, 0.f);
+    tp.b.eps2_hi = (float)(eps2 / (1.0 - g64));
+    if ((double)tp.b.eps2_hi < eps2 / (1.0 - g64)) tp.b.eps2_hi = nextafterf(tp.b.eps2_hi, INFINITY);
+    tp.b.kappa = (float)tc_kappa(d, wide, pr);
+    tp.b.ginf = (float)(1.0 / (1.0 - gd) * (1.0 + 1e-6));
+    tp.b.uR2 = (float)(2.0 * u * R * 1.0001);
+    tp.b.u1 = (float)(u * (1.0 + u) * 1.0001);
+    tp.b.Dp = (float)(1.1 * sqrt(eps2));
+    tp.b.cap = (float)(0.1 * eps2);
+    tp.b.margin = (float)(1e-6 * eps2);
     // MISTIC_TEST_TC_STALL=1 is the failure-detection test: the MMA warp
     // signals nothing, every bounded wait runs out after a short limit, the
     // kernel frees its tensor memory and the call returns MISTIC_ERR_TIMEOUT
@@ -923,7 +1001,8 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   if (use_tc && !tf32_mode) {
     Tuned tu;
     if (tune_lookup(h, o, d, dt, wide, prec, bstart, m, eps2, R, &tu, [&](const TuneCandidate& c, uint32_t S,
-                                                                           double* ms_out, unsigned long long* cands) {
+                                                                           double* ms_out, unsigned long long* cands,
+                                                                           unsigned long long* nunits) {
           EnumParams e2 = ep;
           e2.tc_min = c.tc_min;
           e2.sample = std::max<uint32_t>(S, o.home_sample);
@@ -941,6 +1020,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
           MCK(cudaEventElapsedTime(&t, h->jev[0], h->jev[3]));
           *ms_out = t;
           *cands = totc;
+          *nunits = (unsigned long long)tots[1] + tots[2];
         })) {
       ep.tc_min = tu.tc_min;
       prec_used = tu.prec;
@@ -958,6 +1038,249 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   // ---- join
   set_tc(prec_used);
   point_lists();
+  if (ex && !fp64 && !wide && ex->alloc) {
+    // ---- fused batch: hand the work lists over instead of joining
+    const size_t b_xf = n * (size_t)dpad32 * sizeof(float), b_ids = n * sizeof(uint32_t),
+                 b_bs = ((size_t)m + 1) * sizeof(uint32_t), b_nbr = ((size_t)tots[0] + 1) * sizeof(uint32_t),
+                 b_u = ((size_t)tots[1] + 1) * sizeof(Unit), b_ut = ((size_t)tots[2] + 1) * sizeof(Unit);
+    // host input: its device copy lives in this handle's arena, so it moves too
+    const size_t b_raw = o.input_on_device ? 0 : n * d * esz;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    unsigned char* base = (unsigned char*)ex->alloc(al(b_xf) + al(b_ids) + al(b_bs) + al(b_nbr) + al(b_u) +
+                                                    al(b_ut) + al(b_raw));
+    if (base) {
+      unsigned char* p = base;
+      float* e_xf = (float*)p;
+      p += al(b_xf);
+      uint32_t* e_ids = (uint32_t*)p;
+      p += al(b_ids);
+      uint32_t* e_bs = (uint32_t*)p;
+      p += al(b_bs);
+      uint32_t* e_nbr = (uint32_t*)p;
+      p += al(b_nbr);
+      Unit* e_u = (Unit*)p;
+      p += al(b_u);
+      Unit* e_ut = (Unit*)p;
+      p += al(b_ut);
+      const void* e_raw = x;
+      if (b_raw) {
+        MCK(cudaMemcpyAsync(p, x, b_raw, cudaMemcpyDeviceToDevice, h->stream));
+        e_raw = p;
+      }
+      MCK(cudaMemcpyAsync(e_xf, xf, b_xf, cudaMemcpyDeviceToDevice, h->stream));
+      k_add_u32<<<(unsigned)((n + 255) / 256), 256, 0, h->stream>>>(ids, e_ids, n, ex->row0);
+      launched(h, "add_u32");
+      MCK(cudaMemcpyAsync(e_bs, bstart, b_bs, cudaMemcpyDeviceToDevice, h->stream));
+      MCK(cudaMemcpyAsync(e_nbr, nbr, (size_t)tots[0] * sizeof(uint32_t), cudaMemcpyDeviceToDevice, h->stream));
+      if (tots[1]) MCK(cudaMemcpyAsync(e_u, units, (size_t)tots[1] * sizeof(Unit), cudaMemcpyDeviceToDevice, h->stream));
+      if (tots[2])
+        MCK(cudaMemcpyAsync(e_ut, units_tc, (size_t)tots[2] * sizeof(Unit), cudaMemcpyDeviceToDevice, h->stream));
+      InstDesc& D = ex->desc;
+      D.bstart = e_bs;
+      D.nbr = e_nbr;
+      D.ids = e_ids;
+      D.xs = e_xf;
+      D.raw = e_raw;
+      D.d = d;
+      D.raw_f32 = dt == MISTIC_F32;
+      D.row0 = ex->row0;
+      D.t_lo = t_lo;
+      D.t_hi = t_hi;
+      D.eps2 = eps2;
+      D.amb = jp.amb;
+      D.tcb = tp.b;
+      ex->dpad32 = dpad32;
+      ex->units = e_u;
+      ex->n_units = tots[1];
+      ex->units_tc = e_ut;
+      ex->n_units_tc = tots[2];
+      ex->CH = CH;
+      ex->exported = true;
+      r->tc_operands = (use_tc && tots[2] > 0) ? 1 : 0;
+      MCK(cudaStreamSynchronize(h->stream));  // the arena is reused by this handle's next call
+      r->ms_wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
+      r->kernel_launches = h->launches - launches0;
+      return;
+    }
+  }
+  if (o.ring_capacity > 0) {
+    // ---- streamed pair ring: passes of the join over a fixed ring
+    if (o.csr != MISTIC_PAIRS_NONE || (o.pairs != MISTIC_PAIRS_HOST && !o.pair_sink))
+      throw Error(MISTIC_ERR_INVALID_ARG, "the pair ring streams to host memory or a pair_sink (no CSR table)");
+    const unsigned long long C = o.ring_capacity;
+    const unsigned long long NT = (unsigned long long)tots[1] + tots[2];  // unit tags
+    unsigned long long* ring = abuf<unsigned long long>(h, "ring", C);
+    uint32_t* rtags = abuf<uint32_t>(h, "ring_tags", C);
+    unsigned long long* rout = abuf<unsigned long long>(h, "ring_out", C);
+    uint32_t* rdef = abuf<uint32_t>(h, "ring_deferred", NT + 1);
+    uint32_t* rdef_out = abuf<uint32_t>(h, "ring_def_out", NT + 1);
+    uint32_t* rdin_s = abuf<uint32_t>(h, "ring_def_in_s", (size_t)tots[1] + 1);
+    uint32_t* rdin_t = abuf<uint32_t>(h, "ring_def_in_t", (size_t)tots[2] + 1);
+    unsigned long long* rcount = abuf<unsigned long long>(h, "ring_count", 1);
+    MCK(cudaMemsetAsync(rdef, 0, (NT + 1) * sizeof(uint32_t), h->stream));
+    size_band(totc);
+    uint32_t* btags = abuf<uint32_t>(h, "band_tags", jp.band_cap);
+    unsigned long long* stage = (unsigned long long*)pinned_cache().acquire(C * 8);
+    if (!stage) throw Error(MISTIC_ERR_OUT_OF_MEMORY, "pinned ring staging");
+    std::vector<unsigned long long> all;  // drained pairs (i << 32 | j) when they go to the result
+    unsigned long long total = 0, redone = 0, bandd = 0, amb = 0;
+    uint32_t passes = 0;
+    unsigned long long main_s = 0, main_t = 0;
+    std::vector<uint32_t> din_s, din_t;
+    uint32_t gcap = 0;  // 0: full persistent grids; halved after a pass that finished no unit
+    jp.ring = 1;
+    jp.pairs = ring;
+    jp.cap = C;
+    jp.pair_tags = rtags;
+    jp.band_tags = btags;
+    jp.deferred = rdef;
+    jp.def_out = rdef_out;
+    jp.tag_base_tc = tots[1];
+    auto drain = [&](unsigned long long used) {
+      used = std::min(used, C);
+      if (!used) return;
+      MCK(cudaMemsetAsync(rcount, 0, sizeof(unsigned long long), h->stream));
+      k_ring_drain<<<(unsigned)((used + 255) / 256), 256, 0, h->stream>>>(ring, rtags, rdef, used, rout, rcount);
+      launched(h, "ring_drain");
+      unsigned long long cnt = 0;
+      d2h(h, &cnt, rcount, sizeof cnt);
+      if (!cnt) return;
+      MCK(cudaMemcpyAsync(stage, rout, cnt * 8, cudaMemcpyDeviceToHost, h->stream));
+      MCK(cudaStreamSynchronize(h->stream));
+      total += cnt;
+      if (o.pair_sink) {
+        for (unsigned long long i = 0; i < cnt; ++i) stage[i] = (stage[i] >> 32) | (stage[i] << 32);  // (i, j)
+        o.pair_sink((const uint32_t*)stage, cnt, o.sink_user);
+      } else {
+        all.insert(all.end(), stage, stage + cnt);
+      }
+    };
+    mistic_status rs = MISTIC_OK;
+    try {
+      for (;;) {
+        const bool left_s = main_s < tots[1] || !din_s.empty();
+        const bool left_t = use_tc && (main_t < tots[2] || !din_t.empty());
+        if (!left_s && !left_t) break;
+        if (!din_s.empty())
+          MCK(cudaMemcpyAsync(rdin_s, din_s.data(), din_s.size() * 4, cudaMemcpyHostToDevice, h->stream));
+        if (!din_t.empty())
+          MCK(cudaMemcpyAsync(rdin_t, din_t.data(), din_t.size() * 4, cudaMemcpyHostToDevice, h->stream));
+        MCK(cudaMemsetAsync(ctr, 0, 2 * sizeof(JoinCounters), h->stream));
+        jp.def_in = rdin_s;
+        jp.n_def_in = (uint32_t)din_s.size();
+        jp.main_start = main_s;
+        jp.grid_cap = gcap;
+        tp.def_in = rdin_t;
+        tp.n_def_in = (uint32_t)din_t.size();
+        tp.main_start = main_t;
+        tp.grid_cap = gcap;
+        if (left_s) join::run(h, fp64, CH, jp);
+        if (left_t) {
+          if (wide)
+            join::run_tcw(h, jp, tp);
+          else
+            join::run_tc(h, jp, tp);
+        }
+        JoinCounters c0{}, c1{};
+        d2h(h, &c0, ctr, sizeof c0);
+        d2h(h, &c1, ctr + 1, sizeof c1);
+        if (c0.error || c1.error) throw Error(MISTIC_ERR_TIMEOUT, "a tensor-core tile wait timed out");
+        std::vector<uint32_t> dout(c0.def_n);
+        if (c0.def_n) d2h(h, dout.data(), rdef_out, c0.def_n * 4);
+        // the pairs of units that finished, then the band decisions of their
+        // band entries in slices the ring can hold
+        drain(c0.pairs);
+        const unsigned long long nb = std::min(c0.band_n, jp.band_cap);
+        for (unsigned long long b0 = 0; b0 < nb; b0 += C) {
+          MCK(cudaMemsetAsync(&ctr[0].pairs, 0, sizeof(unsigned long long), h->stream));
+          jp.band0 = b0;
+          jp.band1 = std::min(nb, b0 + C);
+          join::run_band(h, jp);
+          unsigned long long used = 0;
+          d2h(h, &used, &ctr[0].pairs, sizeof used);
+          drain(used);
+        }
+        {
+          JoinCounters cb{};
+          d2h(h, &cb, ctr, sizeof cb);
+          bandd += cb.band;
+          amb += cb.ambiguous;
+        }
+        // cursors: claims past the deferred list came from the main list;
+        // deferred units that were never claimed are carried over
+        const unsigned long long cs = c0.next_unit, ct = c1.next_unit;
+        const unsigned long long nds = din_s.size(), ndt = din_t.size();
+        const unsigned long long got_s = left_s ? std::min(cs, nds) + std::min(cs > nds ? cs - nds : 0ull, tots[1] - main_s) : 0;
+        const unsigned long long got_t = left_t ? std::min(ct, ndt) + std::min(ct > ndt ? ct - ndt : 0ull, tots[2] - main_t) : 0;
+        std::vector<uint32_t> ns(din_s.begin() + std::min(cs, nds), din_s.end());
+        std::vector<uint32_t> nt(din_t.begin() + std::min(ct, ndt), din_t.end());
+        if (!left_s) ns = din_s;
+        if (!left_t) nt = din_t;
+        if (left_s) main_s += std::min(cs > nds ? cs - nds : 0ull, tots[1] - main_s);
+        if (left_t) main_t += std::min(ct > ndt ? ct - ndt : 0ull, tots[2] - main_t);
+        for (uint32_t tg : dout) {
+          if (tg < tots[1])
+            ns.push_back(tg);
+          else
+            nt.push_back(tg - tots[1]);
+        }
+        if (c0.def_n) {
+          MCK(cudaMemcpyAsync(rdef_out, dout.data(), dout.size() * 4, cudaMemcpyHostToDevice, h->stream));
+          k_clear_flags<<<(unsigned)((c0.def_n + 255) / 256), 256, 0, h->stream>>>(rdef, rdef_out, c0.def_n);
+          launched(h, "clear_flags");
+        }
+        redone += c0.def_n;
+        ++passes;
+        din_s.swap(ns);
+        din_t.swap(nt);
+        if (got_s + got_t <= c0.def_n) {  // no unit finished: fewer units at a time
+          if (gcap == 1) throw Error(MISTIC_ERR_PAIR_OVERFLOW, "a work unit has more pairs than the pair ring holds");
+          gcap = gcap ? gcap / 2 : (unsigned)std::max(1, h->sms / 2);
+        }
+      }
+    } catch (const Error& e) {
+      pinned_cache().release(stage);
+      throw;
+    }
+    pinned_cache().release(stage);
+    (void)rs;
+    clk.mark();  // 7
+    r->pairs_ij = total;
+    r->pairs_ordered_incl_self = 2 * total + n;
+    r->band_pairs = fp64 ? 0 : bandd;
+    r->ulp_ambiguous = amb;
+    r->ring_passes = passes;
+    r->ring_units_redone = redone;
+    r->tc_operands = (use_tc && tots[2] > 0) ? (wide ? 1 + prec_used : 1) : 0;
+    if (!o.pair_sink) {
+      if (o.sort_pairs) std::sort(all.begin(), all.end());
+      uint32_t* hp = (uint32_t*)pinned_cache().acquire(std::max<size_t>(1, all.size() * 8));
+      if (!hp) hp = (uint32_t*)malloc(std::max<size_t>(1, all.size() * 8));
+      if (!hp) throw Error(MISTIC_ERR_OUT_OF_MEMORY, "host pair buffer");
+      for (size_t i = 0; i < all.size(); ++i) {
+        hp[2 * i] = (uint32_t)(all[i] >> 32);
+        hp[2 * i + 1] = (uint32_t)all[i];
+      }
+      r->pairs = hp;
+      r->pairs_len = all.size();
+      r->pairs_on_device = 0;
+      r->_owner = hp;
+    }
+    clk.mark();  // 8
+    MCK(cudaStreamSynchronize(h->stream));
+    r->ms_h2d = clk.ms(0, 1);
+    r->ms_prep = clk.ms(1, 2);
+    r->ms_keys = clk.ms(2, 3);
+    r->ms_sort = clk.ms(3, 4);
+    r->ms_bins = clk.ms(4, 5);
+    r->ms_enum = clk.ms(5, 6);
+    r->ms_join = clk.ms(6, 7);
+    r->ms_d2h = clk.ms(7, 8);
+    r->ms_total = clk.ms(0, 8);
+    r->kernel_launches = h->launches - launches0;
+    r->ms_wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
+    return;
+  }
   const bool want_pairs = o.pairs != MISTIC_PAIRS_NONE;
   const bool want_csr = o.csr != MISTIC_PAIRS_NONE;
   const bool need_pairs = want_pairs || want_csr;  // the CSR table is built from the pair list
@@ -1133,6 +1456,410 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   r->kernel_launches = h->launches - launches0;
   r->ms_wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
   if (tail != MISTIC_OK) throw Error(tail, "pair buffer smaller than the pair count; counts are valid");
+}
+
+// ------------------------------------------------------------------ fused batch join
+// Units of instance i of a class occupy [off[i], off[i+1]) of the class's
+// list: tag each with its instance (index into the batch's InstDesc array).
+__global__ void k_unit_inst(const unsigned long long* __restrict__ off, uint32_t n_inst, const uint32_t* __restrict__ gidx,
+                            uint32_t* __restrict__ unit_inst, unsigned long long total) {
+  const unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  uint32_t lo = 0, hi = n_inst - 1;  // last instance whose first unit is <= t
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  unit_inst[t] = gidx[lo];
+}
+
+// Sorted packed pairs of global row ids -> local ids of their instance
+// (row0 of the instance subtracted from both halves) in memory order (i, j).
+__global__ void k_localize(unsigned long long* __restrict__ p, size_t np, const uint32_t* __restrict__ row0,
+                           uint32_t n_inst) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= np) return;
+  const unsigned long long v = p[t];
+  const uint32_t gi = (uint32_t)(v >> 32), gj = (uint32_t)v;
+  uint32_t lo = 0, hi = n_inst - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (row0[mid] <= gi) lo = mid; else hi = mid - 1;
+  }
+  const uint32_t r0 = row0[lo];
+  p[t] = ((unsigned long long)(gj - r0) << 32) | (gi - r0);
+}
+
+// All instances of a batch in one pass of the join kernels.  Phase one
+// builds every instance's index and work lists on worker streams
+// (run_selfjoin with a BatchExport) into one batch arena.  Phase two, on the
+// handle's stream and captured as one CUDA graph: per dimensionality class,
+// the instances' unit lists are concatenated and tagged with their instance,
+// one persistent CUDA-core launch and one persistent tensor-core launch drain
+// all of them (each unit reads its instance's rows, bins and thresholds),
+// and one band-decision launch finishes every instance.  Pairs carry global
+// row ids; accepted pairs are counted per instance as they are staged.  The
+// reference runs one process per dataset (script.sh:86-117); its nearest
+// device-side idea is nodeByPoint4's atomic point queue (src/kernel.cu:912-989).
+mistic_status run_batch_fused(mistic_handle h, const mistic_instance* inst, uint32_t m, const mistic_opts& o,
+                              mistic_result* results, unsigned W, std::string* msg) {
+  const auto wall0 = std::chrono::steady_clock::now();
+  // ---- batch arena: bump allocation for the exported work lists
+  std::vector<uint32_t> row0(m);
+  size_t est = 64u << 20;
+  {
+    unsigned long long acc = 0;
+    for (uint32_t i = 0; i < m; ++i) {
+      row0[i] = (uint32_t)acc;
+      acc += inst[i].n;
+      const size_t esz = inst[i].dtype == MISTIC_F64 ? 8 : 4;
+      est += inst[i].n * (((inst[i].d + 3) & ~3u) * 4 + 96 + (o.input_on_device ? 0 : inst[i].d * esz)) + 4096;
+    }
+    if (acc >= 0xffffffffull) return MISTIC_ERR_TOO_LARGE;  // global row ids are 32-bit
+  }
+  unsigned char* arena = (unsigned char*)h->arena.get("batch", est);
+  const size_t arena_bytes = h->arena.bufs["batch"].bytes;
+  size_t arena_used = 0;
+  std::mutex amu;
+  auto alloc = [&](size_t b) -> void* {
+    std::lock_guard<std::mutex> g(amu);
+    b = (b + 255) & ~(size_t)255;
+    if (arena_used + b > arena_bytes) return nullptr;  // that instance is joined on its own instead
+    void* p = arena + arena_used;
+    arena_used += b;
+    return p;
+  };
+  std::vector<BatchExport> ex(m);
+  for (uint32_t i = 0; i < m; ++i) {
+    ex[i].row0 = row0[i];
+    ex[i].alloc = alloc;
+  }
+  // ---- phase one on the worker handles
+  std::atomic<uint32_t> next{0};
+  std::atomic<bool> stop{false};
+  std::mutex mu;
+  uint32_t err_i = UINT32_MAX;
+  mistic_status err_s = MISTIC_OK;
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < W; ++t) {
+    th.emplace_back([&, t]() {
+      mistic_handle w = h->workers[t];
+      cudaSetDevice(h->device);
+      for (;;) {
+        const uint32_t i = next.fetch_add(1);
+        if (i >= m || stop.load()) break;
+        mistic_status s = MISTIC_OK;
+        std::string em;
+        try {
+          run_selfjoin(w, inst[i].pts, inst[i].n, inst[i].d, inst[i].dtype, inst[i].k, inst[i].eps, &o, &results[i],
+                       &ex[i]);
+        } catch (const Error& e) {
+          s = e.status;
+          em = e.what();
+        } catch (const std::exception& e) {
+          s = MISTIC_ERR_INTERNAL;
+          em = e.what();
+        }
+        if (s != MISTIC_OK) {
+          std::lock_guard<std::mutex> g(mu);
+          if (i < err_i) {
+            err_i = i;
+            err_s = s;
+            *msg = em;
+          }
+          stop.store(true);
+        }
+      }
+    });
+  }
+  for (auto& x : th) x.join();
+  if (err_s != MISTIC_OK) return err_s;
+
+  // ---- phase two: classes of exported instances by d
+  std::vector<uint32_t> gl;  // exported instance -> batch index, ascending (so row0 ascends too)
+  for (uint32_t i = 0; i < m; ++i)
+    if (ex[i].exported) gl.push_back(i);
+  if (gl.empty()) return MISTIC_OK;
+  const uint32_t G = (uint32_t)gl.size();
+  std::map<uint32_t, std::vector<uint32_t>> cls;  // d -> positions in gl
+  for (uint32_t g = 0; g < G; ++g) cls[inst[gl[g]].d].push_back(g);
+  unsigned long long tot_u = 0, tot_ut = 0, cand = 0, tot_n = 0;
+  for (uint32_t g = 0; g < G; ++g) {
+    tot_u += ex[gl[g]].n_units;
+    tot_ut += ex[gl[g]].n_units_tc;
+    cand += results[gl[g]].candidates;
+    tot_n += inst[gl[g]].n;
+  }
+  const size_t nc = cls.size();
+  // device tables, allocated before the capture
+  InstDesc* d_desc = abuf<InstDesc>(h, "b_desc", G);
+  uint32_t* d_row0 = abuf<uint32_t>(h, "b_row0", G);
+  unsigned long long* d_ipairs = abuf<unsigned long long>(h, "b_ipairs", G);
+  Unit* d_units = abuf<Unit>(h, "b_units", tot_u + 1);
+  Unit* d_units_tc = abuf<Unit>(h, "b_units_tc", tot_ut + 1);
+  uint32_t* d_uinst = abuf<uint32_t>(h, "b_uinst", tot_u + 1);
+  uint32_t* d_uinst_tc = abuf<uint32_t>(h, "b_uinst_tc", tot_ut + 1);
+  unsigned long long* d_off = abuf<unsigned long long>(h, "b_off", 2 * (G + nc) + 2);
+  uint32_t* d_gidx = abuf<uint32_t>(h, "b_gidx", G + 1);
+  JoinCounters* ctr = abuf<JoinCounters>(h, "b_ctr", 2);
+  {
+    std::vector<InstDesc> hd(G);
+    std::vector<uint32_t> hr(G);
+    for (uint32_t g = 0; g < G; ++g) {
+      hd[g] = ex[gl[g]].desc;
+      hr[g] = ex[gl[g]].desc.row0;
+    }
+    MCK(cudaMemcpyAsync(d_desc, hd.data(), G * sizeof(InstDesc), cudaMemcpyHostToDevice, h->stream));
+    MCK(cudaMemcpyAsync(d_row0, hr.data(), G * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+  }
+  // per class: unit offsets (simt, tc) and the class's instance -> batch table
+  struct Cls {
+    uint32_t d, dpad32;
+    int CH;
+    unsigned long long u0, nu, t0, nt;  // ranges in the batch unit lists
+    unsigned long long* off_u;          // device prefix of unit counts (n_inst + 1)
+    unsigned long long* off_t;
+    uint32_t* gidx;                     // device: class instance -> exported index
+    uint32_t ninst;
+    std::vector<uint32_t> members;
+  };
+  std::vector<Cls> C;
+  {
+    std::vector<unsigned long long> hoff;
+    std::vector<uint32_t> hg;
+    unsigned long long uu = 0, tt = 0;
+    size_t offpos = 0, gpos = 0;
+    for (auto& kv : cls) {
+      Cls c;
+      c.d = kv.first;
+      c.members = kv.second;
+      c.ninst = (uint32_t)kv.second.size();
+      c.dpad32 = ex[gl[kv.second[0]]].dpad32;
+      c.CH = ex[gl[kv.second[0]]].CH;
+      c.u0 = uu;
+      c.t0 = tt;
+      c.off_u = d_off + offpos;
+      c.off_t = d_off + offpos + c.ninst + 1;
+      c.gidx = d_gidx + gpos;
+      unsigned long long a = 0, b = 0;
+      std::vector<unsigned long long> ou(c.ninst + 1), ot(c.ninst + 1);
+      for (uint32_t j = 0; j < c.ninst; ++j) {
+        ou[j] = a;
+        ot[j] = b;
+        a += ex[gl[kv.second[j]]].n_units;
+        b += ex[gl[kv.second[j]]].n_units_tc;
+        hg.push_back(kv.second[j]);
+      }
+      ou[c.ninst] = a;
+      ot[c.ninst] = b;
+      c.nu = a;
+      c.nt = b;
+      hoff.insert(hoff.end(), ou.begin(), ou.end());
+      hoff.insert(hoff.end(), ot.begin(), ot.end());
+      offpos += 2 * (c.ninst + 1);
+      gpos += c.ninst;
+      uu += a;
+      tt += b;
+      C.push_back(std::move(c));
+    }
+    MCK(cudaMemcpyAsync(d_off, hoff.data(), hoff.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                        h->stream));
+    MCK(cudaMemcpyAsync(d_gidx, hg.data(), hg.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+  }
+  // pair list (when wanted) and band list
+  const bool want_pairs = o.pairs != MISTIC_PAIRS_NONE;
+  unsigned long long cap = 0;
+  unsigned long long* pbuf = nullptr;
+  if (want_pairs) {
+    cap = std::max<unsigned long long>(1ull << 20, 16ull * tot_n);
+    auto it = h->arena.bufs.find("b_pairs");
+    if (it != h->arena.bufs.end()) cap = std::max<unsigned long long>(cap, it->second.bytes / 8);
+  }
+  unsigned long long bcap = std::max<unsigned long long>(1ull << 20, 2ull * tot_n);
+  bcap = std::max<unsigned long long>(bcap, std::min<unsigned long long>(cand / 8192, 1ull << 30));
+  {
+    auto it = h->arena.bufs.find("b_band");
+    if (it != h->arena.bufs.end()) bcap = std::max<unsigned long long>(bcap, it->second.bytes / 8);
+    if (const char* e = getenv("MISTIC_BAND_CAP")) bcap = std::max<unsigned long long>(1, strtoull(e, nullptr, 10));
+  }
+  const bool use_graph = !(getenv("MISTIC_BATCH_GRAPH") && *getenv("MISTIC_BATCH_GRAPH") == '0');
+  JoinCounters hc{};
+  std::vector<unsigned long long> ipairs(G);
+  float ms_fused = 0;
+  bool complete = false;
+  for (int attempt = 0; attempt < 3 && !complete; ++attempt) {
+    if (want_pairs) pbuf = abuf<unsigned long long>(h, "b_pairs", cap);
+    unsigned long long* band = abuf<unsigned long long>(h, "b_band", bcap);
+    // ---- the fused pass: recorded into one CUDA graph (or issued directly)
+    auto issue = [&]() {
+      MCK(cudaMemsetAsync(ctr, 0, 2 * sizeof(JoinCounters), h->stream));
+      MCK(cudaMemsetAsync(d_ipairs, 0, G * sizeof(unsigned long long), h->stream));
+      for (const Cls& c : C) {
+        unsigned long long pu = 0, pt = 0;
+        for (uint32_t j = 0; j < c.ninst; ++j) {
+          const BatchExport& e = ex[gl[c.members[j]]];
+          if (e.n_units)
+            MCK(cudaMemcpyAsync(d_units + c.u0 + pu, e.units, e.n_units * sizeof(Unit), cudaMemcpyDeviceToDevice,
+                                h->stream));
+          if (e.n_units_tc)
+            MCK(cudaMemcpyAsync(d_units_tc + c.t0 + pt, e.units_tc, e.n_units_tc * sizeof(Unit),
+                                cudaMemcpyDeviceToDevice, h->stream));
+          pu += e.n_units;
+          pt += e.n_units_tc;
+        }
+        if (c.nu) {
+          k_unit_inst<<<(unsigned)((c.nu + 255) / 256), 256, 0, h->stream>>>(c.off_u, c.ninst, c.gidx,
+                                                                            d_uinst + c.u0, c.nu);
+          launched(h, "unit_inst");
+        }
+        if (c.nt) {
+          k_unit_inst<<<(unsigned)((c.nt + 255) / 256), 256, 0, h->stream>>>(c.off_t, c.ninst, c.gidx,
+                                                                            d_uinst_tc + c.t0, c.nt);
+          launched(h, "unit_inst");
+        }
+      }
+      for (const Cls& c : C) {
+        JoinParams jp{};
+        jp.units = d_units + c.u0;
+        jp.n_units = c.nu;
+        jp.dpad = c.dpad32;
+        jp.d = c.d;
+        jp.pairs = pbuf;
+        jp.cap = cap;
+        jp.band_list = band;
+        jp.band_cap = bcap;
+        jp.ctr = ctr;
+        jp.insts = d_desc;
+        jp.unit_inst = d_uinst + c.u0;
+        jp.inst_row0 = d_row0;
+        jp.n_inst = G;
+        jp.inst_pairs = d_ipairs;
+        // each launch drains its own list from the start
+        MCK(cudaMemsetAsync(&ctr[0].next_unit, 0, sizeof(unsigned long long), h->stream));
+        MCK(cudaMemsetAsync(&ctr[1].next_unit, 0, sizeof(unsigned long long), h->stream));
+        join::run(h, false, c.CH, jp);
+        if (c.nt) {
+          TcParams tp{};
+          tp.units = d_units_tc + c.t0;
+          tp.n_units = c.nt;
+          tp.ctr = ctr + 1;
+          tp.unit_inst = d_uinst_tc + c.t0;
+          tp.b = ex[gl[c.members[0]]].desc.tcb;  // per unit from its instance in the kernel
+          tp.wait_limit = 2000000000ll;
+          tp.prec = 0;
+          join::run_tc(h, jp, tp);
+        }
+      }
+      JoinParams jb{};
+      jb.ctr = ctr;
+      jb.pairs = pbuf;
+      jb.cap = cap;
+      jb.band_list = band;
+      jb.band_cap = bcap;
+      jb.insts = d_desc;
+      jb.inst_row0 = d_row0;
+      jb.n_inst = G;
+      jb.inst_pairs = d_ipairs;
+      join::run_band(h, jb);
+    };
+    MCK(cudaEventRecord(h->jev[0], h->stream));
+    if (use_graph) {
+      cudaGraph_t graph = nullptr;
+      cudaGraphExec_t exec = nullptr;
+      MCK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        issue();
+      } catch (...) {
+        cudaStreamEndCapture(h->stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        throw;
+      }
+      MCK(cudaStreamEndCapture(h->stream, &graph));
+      const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      MCK(ie);
+      const cudaError_t le = cudaGraphLaunch(exec, h->stream);
+      cudaGraphExecDestroy(exec);  // destruction waits for nothing: the launch is already queued
+      MCK(le);
+    } else {
+      issue();
+    }
+    MCK(cudaEventRecord(h->jev[1], h->stream));
+    MCK(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, h->stream));
+    MCK(cudaMemcpyAsync(ipairs.data(), d_ipairs, G * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+    MCK(cudaStreamSynchronize(h->stream));
+    MCK(cudaEventElapsedTime(&ms_fused, h->jev[0], h->jev[1]));
+    JoinCounters tcc{};
+    MCK(cudaMemcpy(&tcc, ctr + 1, sizeof tcc, cudaMemcpyDeviceToHost));
+    if (hc.error || tcc.error) throw Error(MISTIC_ERR_TIMEOUT, "a tensor-core tile wait timed out");
+    if (hc.band_n > bcap) {
+      bcap = hc.band_n + hc.band_n / 4;
+      continue;
+    }
+    if (want_pairs && hc.pairs > cap) {
+      cap = hc.pairs + hc.pairs / 8;
+      continue;
+    }
+    complete = true;
+  }
+  if (!complete) throw Error(MISTIC_ERR_INTERNAL, "the fused batch join still overflowed after its last pass");
+  // ---- per-instance results
+  std::vector<unsigned long long> pstart(G + 1, 0);
+  if (want_pairs && hc.pairs) {
+    uint64_t* pk[2] = {(uint64_t*)pbuf, abuf<uint64_t>(h, "b_pairs_tmp", hc.pairs)};
+    uint32_t* pv[2] = {nullptr, nullptr};
+    const int c = radix_sort_u64(h, pk, pv, false, false, hc.pairs, 32 + bit_length(tot_n ? row0.back() + inst[m - 1].n : 1));
+    unsigned long long* sorted = (unsigned long long*)pk[c];
+    for (uint32_t g = 0; g < G; ++g) pstart[g + 1] = pstart[g] + ipairs[g];
+    if (pstart[G] != hc.pairs) throw Error(MISTIC_ERR_INTERNAL, "per-instance pair counts do not add up");
+    k_localize<<<(unsigned)((hc.pairs + 255) / 256), 256, 0, h->stream>>>(sorted, hc.pairs, d_row0, G);
+    launched(h, "localize");
+    unsigned long long* host_all = nullptr;
+    if (o.pairs == MISTIC_PAIRS_HOST) {
+      host_all = (unsigned long long*)malloc(hc.pairs * 8);
+      if (!host_all) throw Error(MISTIC_ERR_OUT_OF_MEMORY, "host pair buffer");
+      MCK(cudaMemcpyAsync(host_all, sorted, hc.pairs * 8, cudaMemcpyDeviceToHost, h->stream));
+    }
+    MCK(cudaStreamSynchronize(h->stream));
+    for (uint32_t g = 0; g < G; ++g) {
+      mistic_result& r = results[gl[g]];
+      const unsigned long long np = ipairs[g];
+      r.pairs_len = np;
+      if (o.pairs == MISTIC_PAIRS_HOST) {
+        uint32_t* hp = (uint32_t*)pinned_cache().acquire(std::max<size_t>(1, np * 8));
+        if (!hp) hp = (uint32_t*)malloc(std::max<size_t>(1, np * 8));
+        if (!hp) {
+          free(host_all);
+          throw Error(MISTIC_ERR_OUT_OF_MEMORY, "host pair buffer");
+        }
+        memcpy(hp, host_all + pstart[g], np * 8);
+        r.pairs = hp;
+        r.pairs_on_device = 0;
+        r._owner = hp;
+      } else {
+        void* dp = nullptr;
+        MCK(cudaMalloc(&dp, std::max<size_t>(8, np * 8)));
+        MCK(cudaMemcpyAsync(dp, sorted + pstart[g], np * 8, cudaMemcpyDeviceToDevice, h->stream));
+        r.pairs = (uint32_t*)dp;
+        r.pairs_on_device = 1;
+        r._owner = dp;
+      }
+    }
+    free(host_all);
+    MCK(cudaStreamSynchronize(h->stream));
+  }
+  const double wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
+  for (uint32_t g = 0; g < G; ++g) {
+    mistic_result& r = results[gl[g]];
+    r.pairs_ij = ipairs[g];
+    r.pairs_ordered_incl_self = 2 * ipairs[g] + r.n;
+    r.ms_join = ms_fused;  // the fused join pass is shared by all instances of the batch
+    r.ms_wall = wall;
+    r.ulp_ambiguous = 0;
+    r.band_pairs = 0;
+  }
+  return MISTIC_OK;
 }
 
 }  // namespace
@@ -1331,7 +2058,19 @@ mistic_status mistic_batch_selfjoin(mistic_handle h, const mistic_instance* inst
   unsigned want = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
   if (const char* e = getenv("MISTIC_BATCH_STREAMS")) want = (unsigned)std::max(1l, strtol(e, nullptr, 10));
   const unsigned W = std::min<unsigned>(want, m);
-  if (W <= 1 || (opts && opts->pair_buffer)) {
+  mistic_opts o;
+  mistic_opts_init(&o);
+  if (opts) {
+    if (opts->struct_size != sizeof(mistic_opts))
+      return fail(h, MISTIC_ERR_INVALID_ARG, "mistic_opts.struct_size mismatch (call mistic_opts_init)");
+    o = *opts;
+  }
+  // fused: every instance's units drained by shared persistent launches
+  // (run_batch_fused); MISTIC_BATCH_FUSED=0 keeps one pipeline per instance
+  const char* fz = getenv("MISTIC_BATCH_FUSED");
+  const bool fused = m > 1 && !(fz && *fz == '0') && !o.pair_buffer && o.csr == MISTIC_PAIRS_NONE &&
+                     (o.mode == MISTIC_MODE_AUTO || o.mode == MISTIC_MODE_BF16 || o.mode == MISTIC_MODE_FP32);
+  if (!fused && (W <= 1 || o.pair_buffer)) {
     for (uint32_t i = 0; i < m; ++i) {
       mistic_status s = mistic_selfjoin(h, inst[i].pts, inst[i].n, inst[i].d, inst[i].dtype, inst[i].k,
                                         inst[i].eps, opts, &results[i]);
@@ -1353,6 +2092,27 @@ mistic_status mistic_batch_selfjoin(mistic_handle h, const mistic_instance* inst
     for (unsigned t = 0; t < W; ++t) MCK(cudaStreamWaitEvent(h->workers[t]->stream, h->batch_ev, 0));
   } catch (const Error& e) {
     return fail(h, e.status, e.what());
+  }
+  if (fused) {
+    std::string msg;
+    mistic_status st = MISTIC_OK;
+    try {
+      st = mistic::run_batch_fused(h, inst, m, o, results, std::max(1u, W), &msg);
+    } catch (const Error& e) {
+      st = e.status;
+      msg = e.what();
+    } catch (const std::bad_alloc&) {
+      st = MISTIC_ERR_OUT_OF_MEMORY;
+      msg = "host allocation failed";
+    } catch (const std::exception& e) {
+      st = MISTIC_ERR_INTERNAL;
+      msg = e.what();
+    }
+    if (st != MISTIC_OK) {
+      for (uint32_t i = 0; i < m; ++i) mistic_result_free(&results[i]);
+      return fail(h, st, msg.empty() ? mistic_strerror(st) : msg.c_str());
+    }
+    return MISTIC_OK;
   }
   std::atomic<uint32_t> next{0};
   std::atomic<bool> stop{false};

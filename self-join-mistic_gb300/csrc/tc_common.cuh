@@ -138,7 +138,7 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
 // filter, from the unit's largest |a|^2 and this column's |q|^2 (FP32,
 // rounded outward).  Returns false when the bound is too wide to decide
 // anything (the column is then re-decided entirely in FP64).
-__device__ __forceinline__ bool column_threshold(const TcParams& T, float ra2max, float nq2, float* tcol,
+__device__ __forceinline__ bool column_threshold(const TcBound& T, float ra2max, float nq2, float* tcol,
                                                  float* dlt) {
   const float ra = sqrtf(ra2max * T.ginf), rq = sqrtf(nq2 * T.ginf);
   const float rs = ra + rq;

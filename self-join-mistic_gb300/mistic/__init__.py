@@ -56,6 +56,8 @@ class JoinResult:
     tc_operands: str = "none"                # tensor-core operands: none, split-bf16, bf16, tf32
     tc_min_bin: int = 0                      # smallest home bin on the tensor cores
     tuned: bool = False                      # threshold / operands from the autotuner
+    ring_passes: int = 0                     # ring mode: join passes
+    ring_units_redone: int = 0               # ring mode: units run again after the ring filled
     extra: dict = field(default_factory=dict)
 
 
@@ -95,7 +97,8 @@ class Handle:
 
     def opts(self, mode="auto", rp="pca", seed=0, pairs="none", sort_pairs=False,
              pair_capacity=0, input_on_device=False, check_finite=True, timing=True,
-             rp_user=None, pair_buffer=None, csr="none", home_sample=0, autotune=0) -> L.Opts:
+             rp_user=None, pair_buffer=None, csr="none", home_sample=0, autotune=0,
+             ring_capacity=0) -> L.Opts:
         o = L.Opts()
         self.lib.mistic_opts_init(ctypes.byref(o))
         o.mode = MODES[mode]
@@ -112,6 +115,7 @@ class Handle:
         o.csr = {"none": L.PAIRS_NONE, "host": L.PAIRS_HOST, "device": L.PAIRS_DEVICE}[csr]
         o.home_sample = home_sample
         o.autotune = autotune
+        o.ring_capacity = ring_capacity
         if rp_user is not None:
             self._rp_keep = np.ascontiguousarray(rp_user, dtype=np.float64)
             o.rp_user = self._rp_keep.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
@@ -157,7 +161,8 @@ class Handle:
             ms=ms, kernel_launches=r.kernel_launches, pairs=pairs, device_pairs=dev,
             csr_offsets=csr_off, csr_nbrs=csr_nb,
             tc_operands={0: "none", 1: "split-bf16", 2: "bf16", 3: "tf32"}.get(r.tc_operands, "?"),
-            tc_min_bin=r.tc_min_bin, tuned=bool(r.tuned))
+            tc_min_bin=r.tc_min_bin, tuned=bool(r.tuned), ring_passes=r.ring_passes,
+            ring_units_redone=r.ring_units_redone)
         if not keep_device or not r.pairs_on_device:
             self.lib.mistic_result_free(ctypes.byref(r))
         else:

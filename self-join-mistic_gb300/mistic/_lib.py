@@ -55,6 +55,9 @@ class Opts(ctypes.Structure):
         ("csr", i32),
         ("home_sample", u32),
         ("autotune", i32),
+        ("ring_capacity", u64),
+        ("pair_sink", vp),
+        ("sink_user", vp),
     ]
 
 
@@ -89,6 +92,8 @@ class Result(ctypes.Structure):
         ("tc_operands", i32),
         ("tc_min_bin", u32),
         ("tuned", i32),
+        ("ring_passes", u32),
+        ("ring_units_redone", u64),
         ("_owner", vp),
     ]
 
