@@ -7,10 +7,13 @@
 # Only this recipe reads the reference tree; outputs go to oracle/_ref/ only.
 # The reference headers need BS/KB defined (include/params.cuh) and thrust,
 # so the file is compiled with nvcc as host code; no GPU is touched.
-# Usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+# Usage: oracle/build_ref.sh [reference_root]
+#   reference_root: the first argument, else $MISTIC_REFERENCE_ROOT, else a
+#   checkout named `reference` beside this repository.  Where none exists the
+#   recipe does nothing (the GPU machines have no reference tree).
 set -euo pipefail
-REF=${1:-/root/reference}
 HERE="$(cd "$(dirname "$0")" && pwd)"
+REF=${1:-${MISTIC_REFERENCE_ROOT:-$HERE/../../reference}}
 OUT="$HERE/_ref"
 if [ ! -f "$REF/src/utils.cu" ]; then
   echo "reference source not found at $REF; nothing to build" >&2

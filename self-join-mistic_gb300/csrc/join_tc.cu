@@ -742,18 +742,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
             while (m) {
               const int j = __ffs(m) - 1;
               m &= m - 1;
-              // v[j] without dynamic register indexing: a 5-level select tree
-              uint32_t t16[16], t8[8], t4[4], t2[2];
-#pragma unroll
-              for (int k = 0; k < 16; ++k) t16[k] = (j & 16) ? v[16 + k] : v[k];
-#pragma unroll
-              for (int k = 0; k < 8; ++k) t8[k] = (j & 8) ? t16[8 + k] : t16[k];
-#pragma unroll
-              for (int k = 0; k < 4; ++k) t4[k] = (j & 4) ? t8[4 + k] : t8[k];
-#pragma unroll
-              for (int k = 0; k < 2; ++k) t2[k] = (j & 2) ? t4[2 + k] : t4[k];
-              const float vj = __uint_as_float((j & 1) ? t2[1] : t2[0]);
-              if (vj <= -S.dlt[st][c0 + j])
+              if (pick32(v, j) <= -S.dlt[st][c0 + j])
                 acc_bits |= 1u << j;
               else
                 band_bits |= 1u << j;  // decided later in FP64 (band list)
