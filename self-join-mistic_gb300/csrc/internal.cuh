@@ -107,6 +107,11 @@ struct EnumParams {
   uint32_t tc_min;   // home bins with at least this many points get tensor-core units (0: none)
   uint32_t tc_chunk; // home points per tensor-core unit
   uint32_t sample;   // > 1: only home points of sampled 512-point groups (mistic_opts.home_sample)
+  // prefix table over the first p key fields (p = 0: none): ptab[v] = first
+  // bin whose fields 0 .. p-1, as sum_j field_j * stride[j], are >= v
+  int p;
+  uint32_t stride[MAX_K];
+  const uint32_t* ptab;
 };
 
 // FP32 constants of a tensor-core join's per-column error bound (see
@@ -181,6 +186,7 @@ struct JoinParams {
   uint32_t tag_base_tc;
   unsigned long long band0, band1;   // band decisions of band_list[band0 .. band1) (pair ring)
   uint32_t grid_cap;                 // pair ring: at most this many blocks (0: the persistent grid)
+  unsigned long long claim_cap;      // pair ring: claim indices from this one on take no unit (0: no cap)
   // FP32 pre-decision of band pairs (null inv: every band pair goes to FP64):
   // rows xf32[inv[id]] (sorted FP32 rows, stride dpad32) filtered with the
   // FP32 filter's thresholds t_lo / t_hi before the FP64 predicate
@@ -199,6 +205,7 @@ struct TcParams {
   uint32_t n_def_in;
   unsigned long long main_start;  // pair ring: first unit of `units` not yet claimed
   uint32_t grid_cap;          // pair ring: at most this many CTAs (0: one per SM)
+  unsigned long long claim_cap;  // pair ring: claim indices from this one on take no unit (0: no cap)
   TcBound b;               // per-column bound constants (per instance in fused batch joins)
   long long wait_limit;    // nanoseconds before a barrier wait gives up
   int stall_test;          // failure-detection test: the MMA warp never signals (waits run out)
@@ -282,6 +289,10 @@ void bins(mistic_handle_s*, const uint64_t* keys, size_t n, uint32_t* flags, uin
 void gather(mistic_handle_s*, const void* x, mistic_dtype, size_t n, uint32_t d, const uint32_t* perm,
             const double* center, uint32_t dpad32, float* xf, uint32_t dpad64, double* xd,
             uint32_t* ids, double* norm_part, double* rmax);
+// prefix table of the enumeration (EnumParams p, stride, shift): entries + 1
+// values into ptab
+void prefix_table(mistic_handle_s*, const uint64_t* bkey, uint32_t m, const EnumParams&, uint32_t* ptab,
+                  uint32_t entries);
 void enumerate(mistic_handle_s*, const uint64_t* bkey, const uint32_t* bstart, uint32_t m,
                const EnumParams&, uint32_t* nbr_cnt, uint32_t* unit_cnt, uint32_t* unit_cnt_tc,
                unsigned long long* cand, const uint32_t* nbr_off, const uint32_t* unit_off,

@@ -108,6 +108,7 @@ __device__ __forceinline__ RingPair ring_ctx(const JoinParams& P) {
 // Returns false when the worker has nothing more to do.
 __device__ __forceinline__ bool claim_unit(const JoinParams& P, const RingCtx* rc, unsigned long long t,
                                            unsigned long long* u) {
+  if (P.claim_cap && t >= P.claim_cap) return false;
   unsigned long long v;
   if (t < P.n_def_in) {
     v = P.def_in[t];

@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         const unsigned long long t = atomicAdd(&T.ctr->next_unit, 1ull);
         const unsigned long long uu = t < T.n_def_in ? (unsigned long long)T.def_in[t] : T.main_start + (t - T.n_def_in);
         S.unit = uu;
-        bool go = uu < T.n_units && !*abort_flag;
+        bool go = (T.claim_cap == 0 || t < T.claim_cap) && uu < T.n_units && !*abort_flag;
         if (go && P.ring && *(volatile unsigned long long*)&P.ctr->stop) {  // the ring filled: leave it for the next pass
           const RingCtx rc{P.pair_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
           ring_defer(&rc, P.tag_base_tc + (uint32_t)uu);

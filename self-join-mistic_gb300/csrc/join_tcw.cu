@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(WTHREADS, 1)
         const unsigned long long uu = t < T.n_def_in ? (unsigned long long)T.def_in[t] : T.main_start + (t - T.n_def_in);
         S.unit = uu;
         S.ra2max = 0;
-        bool go = uu < T.n_units && !*abort_flag;
+        bool go = (T.claim_cap == 0 || t < T.claim_cap) && uu < T.n_units && !*abort_flag;
         if (go && P.ring && *(volatile unsigned long long*)&P.ctr->stop) {  // the ring filled: leave it for the next pass
           const RingCtx rc{P.pair_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
           ring_defer(&rc, P.tag_base_tc + (uint32_t)uu);

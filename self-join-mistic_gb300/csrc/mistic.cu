@@ -851,6 +851,26 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   ep.sample = o.home_sample;
   ep.tc_min = use_tc ? tc_min_bin(d, wide) : 0u;
   ep.tc_chunk = use_tc ? (wide ? 256u : join::tc_rows(d)) : 128;
+  // prefix table of the enumeration: the first p <= 5 key fields (3^p
+  // lookups a bin) while the table stays within 16 entries a bin and 2^24
+  {
+    const unsigned long long lim = std::min<unsigned long long>(1ull << 24, 16ull * m + 4096);
+    unsigned long long entries = 1;
+    int p = 0;
+    while (p < std::min(ep.k, 5) && entries * (ep.maxkey[p] + 1ull) <= lim) entries *= ep.maxkey[p] + 1ull, ++p;
+    ep.p = p;
+    ep.ptab = nullptr;
+    if (p > 0) {
+      uint32_t st = 1;
+      for (int j = p - 1; j >= 0; --j) {
+        ep.stride[j] = st;
+        st *= ep.maxkey[j] + 1u;
+      }
+      uint32_t* ptab = abuf<uint32_t>(h, "ptab", (size_t)entries + 1);
+      idx::prefix_table(h, bkey, m, ep, ptab, (uint32_t)entries);
+      ep.ptab = ptab;
+    }
+  }
   uint32_t tots[3] = {0, 0, 0};
   unsigned long long totc = 0;
   uint32_t* nbr = nullptr;
@@ -1127,7 +1147,11 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     uint32_t passes = 0;
     unsigned long long main_s = 0, main_t = 0;
     std::vector<uint32_t> din_s, din_t;
-    uint32_t gcap = 0;  // 0: full persistent grids; halved after a pass that finished no unit
+    // after a pass that finished no unit: grids halved down to one block,
+    // then one unit per kernel (a block of many warps can still hold several
+    // units whose pairs together overfill the ring)
+    uint32_t gcap = 0;            // 0: full persistent grids
+    unsigned long long ccap = 0;  // 0: no cap on claims
     jp.ring = 1;
     jp.pairs = ring;
     jp.cap = C;
@@ -1170,10 +1194,12 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
         jp.n_def_in = (uint32_t)din_s.size();
         jp.main_start = main_s;
         jp.grid_cap = gcap;
+        jp.claim_cap = ccap;
         tp.def_in = rdin_t;
         tp.n_def_in = (uint32_t)din_t.size();
         tp.main_start = main_t;
         tp.grid_cap = gcap;
+        tp.claim_cap = ccap;
         if (left_s) join::run(h, fp64, CH, jp);
         if (left_t) {
           if (wide)
@@ -1208,7 +1234,8 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
         }
         // cursors: claims past the deferred list came from the main list;
         // deferred units that were never claimed are carried over
-        const unsigned long long cs = c0.next_unit, ct = c1.next_unit;
+        const unsigned long long cs = ccap ? std::min(c0.next_unit, ccap) : c0.next_unit;
+        const unsigned long long ct = ccap ? std::min(c1.next_unit, ccap) : c1.next_unit;
         const unsigned long long nds = din_s.size(), ndt = din_t.size();
         const unsigned long long got_s = left_s ? std::min(cs, nds) + std::min(cs > nds ? cs - nds : 0ull, tots[1] - main_s) : 0;
         const unsigned long long got_t = left_t ? std::min(ct, ndt) + std::min(ct > ndt ? ct - ndt : 0ull, tots[2] - main_t) : 0;
@@ -1234,8 +1261,9 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
         din_s.swap(ns);
         din_t.swap(nt);
         if (got_s + got_t <= c0.def_n) {  // no unit finished: fewer units at a time
-          if (gcap == 1) throw Error(MISTIC_ERR_PAIR_OVERFLOW, "a work unit has more pairs than the pair ring holds");
-          gcap = gcap ? gcap / 2 : (unsigned)std::max(1, h->sms / 2);
+          if (ccap == 1) throw Error(MISTIC_ERR_PAIR_OVERFLOW, "a work unit has more pairs than the pair ring holds");
+          if (gcap == 1) ccap = 1;
+          gcap = gcap ? std::max(1u, gcap / 2) : (unsigned)std::max(1, h->sms / 2);
         }
       }
     } catch (const Error& e) {
