@@ -414,6 +414,8 @@ def run_mistic(args, wl) -> None:
     step_roof = step_lower_bound(r, n, d, wl.k, ms, peaks)
     north = None if (args.no_c5 or args.workload == "tiny384") else run_north_star(h, args, dev, stream, peaks)
     cpu = cpu_sample(x, wl.eps, args.cpu_seconds) if not args.no_cpu else None
+    ref_gpu = reference_gpu(x, wl.k, wl.eps, r.pairs_ordered_incl_self, args.ref_gpu_timeout) \
+        if args.ref_gpu else None
     value = job_points_per_s(n, world, ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -434,6 +436,7 @@ def run_mistic(args, wl) -> None:
         "roofline": roof,
         "step_roofline": step_roof,
         "north_star": north,
+        "reference_gpu": ref_gpu,
         "e2e": {"value": job_points_per_s(n, world, e2e_ms), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": n * d * x.itemsize, "d2h_bytes_per_step": int(r.pairs_ij) * 8,
                 "h2d_ms": statistics.mean(t[1] for t in e2e_res), "d2h_ms": statistics.mean(t[2] for t in e2e_res)},
@@ -447,6 +450,50 @@ def run_mistic(args, wl) -> None:
     }
     print(json.dumps(line), flush=True)
     h.close()
+
+
+def reference_gpu(x: np.ndarray, k: int, eps: float, ours_ordered: int, timeout: float) -> dict | None:
+    """The reference's own GPU join (build/main of the reference, built for
+    sm_103a by oracle/build_ref_gpu.sh, one binary per DIM) on the same
+    points as an FP64 file: its "Total results Set Size" (ordered pairs
+    including self pairs, src/launcher.cu:3513), "Kernel Time" and "Total
+    Time" (index build + join, file read excluded, src/main.cu:444).  It
+    always builds its own 6 index layers (numRP is not read, src/main.cu:174).
+    None when no binary was built for this d."""
+    d = x.shape[1]
+    exe = os.path.join(ROOT, "oracle", "_ref", f"ref_main_d{d}")
+    if not os.path.exists(exe):
+        return None
+    with tempfile.TemporaryDirectory() as td:
+        fn = os.path.join(td, "points.bin")
+        np.ascontiguousarray(x, dtype=np.float64).tofile(fn)
+        t0 = time.perf_counter()
+        try:
+            pr = subprocess.run([exe, fn, str(d), str(k), repr(float(eps))], capture_output=True, text=True,
+                                timeout=timeout)
+        except subprocess.TimeoutExpired:
+            return {"status": f"not finished within {timeout:.0f} s"}
+        wall = time.perf_counter() - t0
+    out = pr.stdout
+
+    def grab(tag):
+        for line in out.splitlines():
+            if line.startswith(tag):
+                try:
+                    return float(line[len(tag):].split()[0])
+                except ValueError:
+                    return None
+        return None
+
+    total = grab("Total results Set Size:")
+    res = {"status": "ok" if pr.returncode == 0 else f"exit {pr.returncode}",
+           "ordered_pairs_incl_self": None if total is None else int(total),
+           "kernel_s": grab("Kernel Time:"), "total_s": grab("Total Time:"), "process_wall_s": wall,
+           "same_count": None if total is None else int(total) == int(ours_ordered),
+           "binary": os.path.relpath(exe, ROOT)}
+    if pr.returncode != 0:
+        res["stderr_tail"] = pr.stderr[-400:]
+    return res
 
 
 def step_lower_bound(r, n: int, d: int, k: int, ms: float, peaks: dict) -> dict:
@@ -736,6 +783,9 @@ def main() -> None:
     ap.add_argument("--c5-sample-cands", type=float, default=1.5e10,
                     help="candidate pairs of the north-star mixed/FP64 sample")
     ap.add_argument("--ref-seconds", type=float, default=6.0)
+    ap.add_argument("--ref-gpu", action="store_true",
+                    help="also run the reference's own GPU build (oracle/build_ref_gpu.sh) on the same points")
+    ap.add_argument("--ref-gpu-timeout", type=float, default=900.0)
     args = ap.parse_args()
     if args.workload == "batch2000":
         if args.impl == "reference":

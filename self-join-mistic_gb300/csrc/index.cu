@@ -11,12 +11,11 @@
 //    sorted, and non-empty bins become contiguous runs of the sorted order.
 //  - the 3^k neighbour search over sorted bin keys, generateRanges /
 //    binarySearch in src/tree.cu:596-759,886-996 (device form
-//    GPUBinarySearch, src/kernel.cu:164-224).  Here one warp per non-empty
-//    bin resolves the top key fields of its ±1 neighbourhood through a
-//    direct-address prefix table and the rest by coalesced scans of short
-//    sorted ranges (warp searches narrow long ones field by field), so empty
-//    prefixes cost nothing; only neighbours of index >= the home bin are
-//    emitted (each unordered bin pair once).
+//    GPUBinarySearch, src/kernel.cu:164-224).  Here one thread per non-empty
+//    bin walks the ±1 neighbourhood depth-first, narrowing a sorted range one
+//    key field at a time (the top fields through a direct-address prefix
+//    table), so empty prefixes are pruned early; only neighbours of index >=
+//    the home bin are emitted (each unordered bin pair once).
 #include <math.h>
 
 #include "internal.cuh"
@@ -327,46 +326,31 @@ __global__ void k_max_final(const double* __restrict__ part, uint32_t nparts, do
 }
 
 // ------------------------------------------------------------ neighbour enumeration
-// One warp per non-empty home bin h.  Its neighbours are the bins whose key
-// fields each differ from h's by at most one and whose index is >= h (each
-// unordered bin pair once); they come out in ascending bin order, starting
-// with h itself.
+// One thread per non-empty bin h.  Depth-first over the key fields: at
+// level j the candidate field value is K_j - 1, K_j, K_j + 1; the bins whose
+// key starts with the chosen prefix form a contiguous sorted range, found by
+// two lower-bound searches inside the parent range.  The first p fields
+// skip the searches: a direct-address table (ptab[v] = first bin whose
+// p-field prefix, read as a mixed-radix number, is >= v) gives the range of
+// each of the 3^p prefixes with two loads, and the walk starts at level p
+// inside it.  A range lying wholly below h is skipped (home <= neighbour).
+// Leaves come out in ascending bin order, starting with h itself.
 //
-// Top fields: a direct-address table over the first p key fields (ptab[v] =
-// first bin whose p-field prefix, read as a mixed-radix number, is >= v)
-// turns each of the 3^p prefixes of the ±1 neighbourhood into a sorted bin
-// range with two loads; the lanes look up 32 prefixes at a time.
-// Remaining fields: a range of at most ENUM_LIN bins is scanned with
-// coalesced loads, each lane testing the remaining fields of one bin; a
-// longer range is narrowed one field at a time, depth first, by 32-way warp
-// searches over the sorted keys.  Without a table (p = 0) the narrowing
-// starts at the first field over all bins.
-//
-// Pass 1 (FILL false) counts neighbours, join work units and candidate
+// Pass 1 (fill == false) counts neighbours, join work units and candidate
 // pairs per home bin; pass 2 writes the neighbour list and the units.  The
 // neighbour list of h is cut into segments of about `seg_cap` candidate
 // points, and the home bin into chunks of `chunk` points; one unit is one
 // (chunk, segment) combination.
-constexpr uint32_t ENUM_LIN = 96;  // ranges of at most this many bins are scanned linearly
-constexpr int ENUM_WARPS = 8;      // home bins per block
-
-// First index of [lo, hi) whose key is >= v, or hi.  Warp-collective with
-// uniform arguments: each round probes 32 evenly spaced keys and keeps the
-// segment that holds the answer.
-__device__ __forceinline__ uint32_t warp_lower_bound(const uint64_t* __restrict__ a, uint32_t lo, uint32_t hi,
-                                                     uint64_t v, uint32_t lane) {
-  while (hi - lo > 32) {
-    const uint32_t step = (hi - lo + 31) >> 5;
-    const unsigned long long i = (unsigned long long)lo + (unsigned long long)(lane + 1) * step - 1;
-    const bool lt = i < hi && a[i] < v;
-    const uint32_t c = __popc(__ballot_sync(FULL_MASK, lt));  // leading segments wholly below v
-    const uint32_t nlo = lo + c * step;
-    hi = (uint32_t)min((unsigned long long)hi, (unsigned long long)nlo + step - 1);
-    lo = nlo;
+__device__ __forceinline__ uint32_t lower_bound_u64(const uint64_t* __restrict__ a, uint32_t lo,
+                                                    uint32_t hi, uint64_t v) {
+  while (lo < hi) {
+    uint32_t mid = lo + ((hi - lo) >> 1);
+    if (a[mid] < v)
+      lo = mid + 1;
+    else
+      hi = mid;
   }
-  const uint32_t i = lo + lane;
-  const bool lt = i < hi && a[i] < v;
-  return lo + __popc(__ballot_sync(FULL_MASK, lt));
+  return lo;
 }
 
 // Home-point sample (mistic_opts.home_sample): group g (points
@@ -384,16 +368,14 @@ __device__ __forceinline__ bool group_sampled(uint32_t h, uint32_t g, uint32_t S
 }
 
 template <bool FILL>
-__global__ void __launch_bounds__(ENUM_WARPS * 32)
-    k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __restrict__ bstart, uint32_t m, EnumParams P,
-           uint32_t* __restrict__ nbr_cnt, uint32_t* __restrict__ unit_cnt, uint32_t* __restrict__ unit_cnt_tc,
-           unsigned long long* __restrict__ cand, const uint32_t* __restrict__ nbr_off,
-           const uint32_t* __restrict__ unit_off, const uint32_t* __restrict__ unit_off_tc,
-           uint32_t* __restrict__ nbr, Unit* __restrict__ units_simt, Unit* __restrict__ units_tc) {
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t hb = blockIdx.x * ENUM_WARPS + (threadIdx.x >> 5);
-  if (hb >= m) return;  // whole warps
-  const uint32_t lt_mask = (1u << lane) - 1u;
+__global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __restrict__ bstart,
+                       uint32_t m, EnumParams P, uint32_t* __restrict__ nbr_cnt,
+                       uint32_t* __restrict__ unit_cnt, uint32_t* __restrict__ unit_cnt_tc,
+                       unsigned long long* __restrict__ cand, const uint32_t* __restrict__ nbr_off,
+                       const uint32_t* __restrict__ unit_off, const uint32_t* __restrict__ unit_off_tc,
+                       uint32_t* __restrict__ nbr, Unit* __restrict__ units_simt, Unit* __restrict__ units_tc) {
+  const uint32_t hb = blockIdx.x * blockDim.x + threadIdx.x;
+  if (hb >= m) return;
   const uint64_t K = bkey[hb];
   const uint32_t asz = bstart[hb + 1] - bstart[hb];
   // large home bins go to the tensor-core join (128-row chunks), the rest to the CUDA-core join
@@ -417,190 +399,140 @@ __global__ void __launch_bounds__(ENUM_WARPS * 32)
     }
   }
 
-  // lane j < k holds key field j: its shift, bit width (field j spans
-  // [shift[j], shift[j-1]), shift[-1] = 64), largest value and h's value
-  int f_sh = 0, f_w = 0;
-  uint32_t f_max = 0, f_h = 0;
-  if ((int)lane < P.k) {
-    f_sh = P.shift[lane];
-    f_w = min((lane == 0 ? 64 : P.shift[lane - 1]) - f_sh, 63);
-    f_max = P.maxkey[lane];
-    f_h = (uint32_t)((K >> f_sh) & ((1ull << f_w) - 1ull));
+  int kf[MAX_K];
+  // decode fields: field j spans [shift[j], shift[j-1]) (shift[-1] = 64)
+  for (int j = 0; j < P.k; ++j) {
+    const int hi_bit = j == 0 ? 64 : P.shift[j - 1];
+    const int width = hi_bit - P.shift[j];
+    const uint64_t mask = width >= 64 ? ~0ull : ((1ull << width) - 1ull);
+    kf[j] = (int)((K >> P.shift[j]) & mask);
   }
 
-  uint32_t cnt = 0, nseg = 0, seg_begin = 0;
-  unsigned long long seg_fill = 0, cl = 0;  // cl: this lane's share of the candidate count
-  const uint32_t nb0 = FILL ? nbr_off[hb] : 0u;
-  uint32_t w_nbr = nb0;
-  uint32_t w_unit = FILL ? (tc ? unit_off_tc[hb] : unit_off[hb]) : 0u;
+  uint32_t lo[MAX_K + 1], hi[MAX_K + 1];
+  uint64_t base[MAX_K + 1];
+  int di[MAX_K + 1];
+  lo[0] = 0;
+  hi[0] = m;
+  base[0] = 0;
+  di[0] = 0;
+  int j = 0;
 
-  // units of the segment [s0, s1) of the neighbour list, one per sampled chunk
-  auto emit_units = [&](uint32_t s0, uint32_t s1) {
-    for (uint32_t ch0 = 0; ch0 < nchunks; ch0 += 32) {
-      const uint32_t ch = ch0 + lane;
-      const bool tk = ch < nchunks && group_sampled(hb, ch * csz / SAMPLE_GROUP, P.sample);
-      const uint32_t bm = __ballot_sync(FULL_MASK, tk);
-      if (tk) units[w_unit + __popc(bm & lt_mask)] = Unit{hb, ch, nb0 + s0, nb0 + s1};
-      w_unit += __popc(bm);
-    }
-  };
-  auto close_segment = [&]() {
-    if (FILL) emit_units(seg_begin, cnt);
-    ++nseg;
-    seg_fill = 0;
-    seg_begin = cnt;
-  };
-  // Neighbour bins a of the lanes in hm (ascending with the lane): candidate
-  // count, segment split and, in pass 2, the neighbour list and the units.
-  auto take = [&](uint32_t hm, uint32_t a) {
-    if (hm == 0) return;
-    const bool mine = (hm >> lane) & 1u;
-    uint32_t bsz = 0;
-    if (mine) {
-      bsz = bstart[a + 1] - bstart[a];
-      cl += (a == hb) ? self_s : rows_s * bsz;
-      if (FILL) nbr[w_nbr + __popc(hm & lt_mask)] = a;
-    }
-    const uint32_t nh = __popc(hm);
-    w_nbr += nh;
-    unsigned long long tot = bsz;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL_MASK, tot, o);
-    if (seg_fill + tot <= P.seg_cap) {  // no segment boundary inside this batch
-      seg_fill += tot;
-      cnt += nh;
-      return;
-    }
-    uint32_t mm = hm;
-    while (mm) {
-      const int l = __ffs(mm) - 1;
-      mm &= mm - 1;
-      const uint32_t b = __shfl_sync(FULL_MASK, bsz, l);
-      if (seg_fill > 0 && seg_fill + b > P.seg_cap) close_segment();
-      seg_fill += b;
-      ++cnt;
-    }
-  };
-  // bins of [a, b) (keys sharing fields 0 .. js-1 with a ±1 neighbour
-  // prefix of h) whose fields js .. k-1 are within one of h's
-  auto scan = [&](int js, uint32_t a, uint32_t b) {
-    for (uint32_t s = max(a, hb); s < b; s += 32) {
-      const uint32_t i = s + lane;
-      bool ok = i < b;
-      const uint64_t key = ok ? bkey[i] : 0ull;
-      for (int j = js; j < P.k; ++j) {
-        const int sh = __shfl_sync(FULL_MASK, f_sh, j), w = __shfl_sync(FULL_MASK, f_w, j);
-        const uint32_t fh = __shfl_sync(FULL_MASK, f_h, j);
-        const uint32_t v = (uint32_t)((key >> sh) & ((1ull << w) - 1ull));
-        ok = ok && v + 1u >= fh && v <= fh + 1u;
+  uint32_t cnt = 0, nseg = 0, seg_fill = 0, seg_begin = 0;
+  unsigned long long c = 0;
+  uint32_t w_nbr = FILL ? nbr_off[hb] : 0;
+  uint32_t w_unit = FILL ? (tc ? unit_off_tc[hb] : unit_off[hb]) : 0;
+
+  // Visits neighbour bin `a` (ascending, a >= hb): candidate count, segment
+  // split and, in pass 2, the neighbour list and the units.
+  auto leaf = [&](uint32_t a) {
+    const uint32_t bsz = bstart[a + 1] - bstart[a];
+    c += (a == hb) ? self_s : rows_s * bsz;
+    if (seg_fill > 0 && seg_fill + bsz > P.seg_cap) {
+      if (FILL) {
+        for (uint32_t ch = 0; ch < nchunks; ++ch)
+          if (group_sampled(hb, ch * csz / SAMPLE_GROUP, P.sample))
+            units[w_unit++] = Unit{hb, ch, nbr_off[hb] + seg_begin, nbr_off[hb] + cnt};
       }
-      take(__ballot_sync(FULL_MASK, ok), i);
+      ++nseg;
+      seg_fill = 0;
+      seg_begin = cnt;
     }
-  };
-  // depth-first over fields j0 .. k-1 inside [lo0, hi0), whose keys share the
-  // prefix bits base0 (fields 0 .. j0-1); the level state of depth j lives
-  // in lane j
-  auto descend = [&](int j0, uint32_t lo0, uint32_t hi0, uint64_t base0) {
-    if (hi0 - lo0 <= ENUM_LIN) {
-      scan(j0, lo0, hi0);
-      return;
-    }
-    uint32_t s_lo = 0, s_hi = 0, s_di = 0;
-    uint64_t s_base = 0;
-    if ((int)lane == j0) s_lo = lo0, s_hi = hi0, s_base = base0;
-    int j = j0;
-    while (j >= j0) {
-      const uint32_t di = __shfl_sync(FULL_MASK, s_di, j);
-      if (di == 3) {  // children of this level done (the parent advanced when it descended)
-        --j;
-        continue;
-      }
-      if ((int)lane == j) ++s_di;
-      const int sh = __shfl_sync(FULL_MASK, f_sh, j);
-      const uint32_t fh = __shfl_sync(FULL_MASK, f_h, j), fm = __shfl_sync(FULL_MASK, f_max, j);
-      const int cv = (int)fh + (int)di - 1;
-      if (cv < 0 || (uint32_t)cv > fm) continue;
-      const uint32_t lo = __shfl_sync(FULL_MASK, s_lo, j), hi = __shfl_sync(FULL_MASK, s_hi, j);
-      const uint64_t lower = __shfl_sync(FULL_MASK, s_base, j) | ((uint64_t)cv << sh);
-      const uint64_t upper = lower + (1ull << sh);
-      const uint32_t a = warp_lower_bound(bkey, lo, hi, lower, lane);
-      const uint32_t b = warp_lower_bound(bkey, a, hi, upper, lane);
-      if (a == b || b <= hb) continue;
-      if (j == P.k - 1) {  // all fields fixed: the single bin a (>= hb, as b = a + 1 > hb)
-        take(1u, a);
-        continue;
-      }
-      if (b - a <= ENUM_LIN) {
-        scan(j + 1, a, b);
-        continue;
-      }
-      ++j;
-      if ((int)lane == j) s_lo = a, s_hi = b, s_di = 0, s_base = lower;
-    }
+    seg_fill += bsz;
+    if (FILL) nbr[w_nbr++] = a;
+    ++cnt;
   };
 
+  // the walk below level j0 of the range [lo[j0], hi[j0]) with prefix base[j0]
+  auto walk = [&](int j0) {
+  j = j0;
+  while (j >= j0) {
+    if (di[j] == 3) {
+      --j;
+      if (j >= j0) ++di[j];
+      continue;
+    }
+    const int cv = kf[j] + di[j] - 1;
+    if (cv < 0 || (long long)cv > (long long)P.maxkey[j]) {
+      ++di[j];
+      continue;
+    }
+    const uint64_t lower = base[j] | ((uint64_t)cv << P.shift[j]);
+    const uint64_t upper = lower + (1ull << P.shift[j]);
+    const uint32_t a = lower_bound_u64(bkey, lo[j], hi[j], lower);
+    const uint32_t b = lower_bound_u64(bkey, a, hi[j], upper);
+    if (a == b || b <= hb) {
+      ++di[j];
+      continue;
+    }
+    if (j == P.k - 1) {
+      leaf(a);  // b == a + 1 and a >= hb
+      ++di[j];
+      continue;
+    }
+    base[j + 1] = lower;
+    lo[j + 1] = a;
+    hi[j + 1] = b;
+    di[j + 1] = 0;
+    ++j;
+  }
+  };
   if (P.k == 0) {
-    take(1u, hb);  // no key fields: one bin holding every point
+    leaf(hb);  // no key fields: one bin holding every point
   } else if (P.p == 0) {
-    descend(0, 0, m, 0ull);
+    walk(0);
   } else {
+    // prefixes in ascending order: field j offset by digit j of c in base 3
+    // (field 0 most significant)
     uint32_t n3 = 1;
-    for (int j = 0; j < P.p; ++j) n3 *= 3;
-    for (uint32_t c0 = 0; c0 < n3; c0 += 32) {
-      // lane: prefix c0 + lane, field j offset by digit j of it in base 3
-      // (field 0 most significant), so ranges come in ascending order
-      const uint32_t c = c0 + lane;
-      bool ok = c < n3;
-      uint32_t idx = 0, rem = c, pw = n3 / 3;
-      uint64_t base = 0;
-      for (int j = 0; j < P.p; ++j) {
+    for (int q = 0; q < P.p; ++q) n3 *= 3;
+    for (uint32_t c = 0; c < n3; ++c) {
+      uint32_t rem = c, pw = n3 / 3, idx = 0;
+      uint64_t pre = 0;
+      bool ok = true;
+      for (int q = 0; q < P.p; ++q) {
         const uint32_t t = rem / pw;
         rem -= t * pw;
         pw /= 3;
-        const int sh = __shfl_sync(FULL_MASK, f_sh, j);
-        const uint32_t fh = __shfl_sync(FULL_MASK, f_h, j), fm = __shfl_sync(FULL_MASK, f_max, j);
-        const int cv = (int)fh + (int)t - 1;
-        ok = ok && cv >= 0 && (uint32_t)cv <= fm;
-        const uint32_t v = cv < 0 ? 0u : (uint32_t)cv;
-        idx += v * P.stride[j];
-        base |= (uint64_t)v << sh;
+        const int cv = kf[q] + (int)t - 1;
+        if (cv < 0 || (uint32_t)cv > P.maxkey[q]) {
+          ok = false;
+          break;
+        }
+        idx += (uint32_t)cv * P.stride[q];
+        pre |= (uint64_t)cv << P.shift[q];
       }
-      uint32_t r0 = 0, r1 = 0;
-      if (ok) {
-        r0 = P.ptab[idx];
-        r1 = P.ptab[idx + 1];
-      }
-      ok = ok && r1 > r0 && r1 > hb;
-      uint32_t mk = __ballot_sync(FULL_MASK, ok);
-      if (P.p == P.k) {  // every field fixed: each range is one bin, r0 >= hb
-        take(mk, r0);
+      if (!ok) continue;
+      const uint32_t r0 = P.ptab[idx], r1 = P.ptab[idx + 1];
+      if (r0 == r1 || r1 <= hb) continue;
+      if (P.p == P.k) {  // every field fixed: the single bin r0 (>= hb)
+        leaf(r0);
         continue;
       }
-      while (mk) {
-        const int l = __ffs(mk) - 1;
-        mk &= mk - 1;
-        descend(P.p, __shfl_sync(FULL_MASK, r0, l), __shfl_sync(FULL_MASK, r1, l), __shfl_sync(FULL_MASK, base, l));
-      }
+      lo[P.p] = r0;
+      hi[P.p] = r1;
+      base[P.p] = pre;
+      di[P.p] = 0;
+      walk(P.p);
     }
   }
   if (cnt > 0) {
-    if (FILL) emit_units(seg_begin, cnt);
+    if (FILL) {
+      for (uint32_t ch = 0; ch < nchunks; ++ch)
+        if (group_sampled(hb, ch * csz / SAMPLE_GROUP, P.sample))
+          units[w_unit++] = Unit{hb, ch, nbr_off[hb] + seg_begin, nbr_off[hb] + cnt};
+    }
     ++nseg;
   }
   if (!FILL) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) cl += __shfl_xor_sync(FULL_MASK, cl, o);
-    if (lane == 0) {
-      // a bin's unit count saturates at 2^32 - 1; the 64-bit totals of the
-      // three count arrays (k_count_totals) then exceed the 32-bit offsets the
-      // work lists use, and the call fails with MISTIC_ERR_TOO_LARGE
-      const unsigned long long nu = (unsigned long long)nseg * nchunks_s;
-      const uint32_t nu32 = nu > 0xffffffffull ? 0xffffffffu : (uint32_t)nu;
-      nbr_cnt[hb] = cnt;
-      unit_cnt[hb] = tc ? 0u : nu32;
-      unit_cnt_tc[hb] = tc ? nu32 : 0u;
-      cand[hb] = cl;
-    }
+    // a bin's unit count saturates at 2^32 - 1; the 64-bit totals of the
+    // three count arrays (k_count_totals) then exceed the 32-bit offsets the
+    // work lists use, and the call fails with MISTIC_ERR_TOO_LARGE
+    const unsigned long long nu = (unsigned long long)nseg * nchunks_s;
+    const uint32_t nu32 = nu > 0xffffffffull ? 0xffffffffu : (uint32_t)nu;
+    nbr_cnt[hb] = cnt;
+    unit_cnt[hb] = tc ? 0u : nu32;
+    unit_cnt_tc[hb] = tc ? nu32 : 0u;
+    cand[hb] = c;
   }
 }
 
@@ -734,13 +666,13 @@ void enumerate(mistic_handle_s* h, const uint64_t* bkey, const uint32_t* bstart,
                const EnumParams& P, uint32_t* nbr_cnt, uint32_t* unit_cnt, uint32_t* unit_cnt_tc,
                unsigned long long* cand, const uint32_t* nbr_off, const uint32_t* unit_off,
                const uint32_t* unit_off_tc, uint32_t* nbr, Unit* units, Unit* units_tc, bool fill) {
-  const unsigned nb = (m + ENUM_WARPS - 1) / ENUM_WARPS;
+  const unsigned nb = (m + 127) / 128;
   if (!fill)
-    k_enum<false><<<nb, ENUM_WARPS * 32, 0, h->stream>>>(bkey, bstart, m, P, nbr_cnt, unit_cnt, unit_cnt_tc, cand,
-                                                         nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    k_enum<false><<<nb, 128, 0, h->stream>>>(bkey, bstart, m, P, nbr_cnt, unit_cnt, unit_cnt_tc, cand, nullptr,
+                                             nullptr, nullptr, nullptr, nullptr, nullptr);
   else
-    k_enum<true><<<nb, ENUM_WARPS * 32, 0, h->stream>>>(bkey, bstart, m, P, nullptr, nullptr, nullptr, nullptr,
-                                                        nbr_off, unit_off, unit_off_tc, nbr, units, units_tc);
+    k_enum<true><<<nb, 128, 0, h->stream>>>(bkey, bstart, m, P, nullptr, nullptr, nullptr, nullptr, nbr_off,
+                                            unit_off, unit_off_tc, nbr, units, units_tc);
   launched(h, fill ? "enum_fill" : "enum_count");
 }
 

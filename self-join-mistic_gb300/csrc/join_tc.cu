@@ -112,6 +112,7 @@ struct TcShared2 {
   uint32_t abort_flag;
   uint32_t tmem_base;
   uint32_t pflag[2];  // producer-wide decisions, written by producer thread 0
+  float npart[2][2][TM];  // [tile parity][K-block parity][row]: partial row norms of the two threads of a row
   unsigned long long full[NS], sfree[NS], dfull[NACC], dfree[NACC], afull, afree;
 };
 
@@ -123,14 +124,16 @@ __device__ __forceinline__ void prod_sync() { asm volatile("bar.sync 1, %0;" ::"
 // chunk slots of the row itself -- floats [8kb, 8kb+4) into the hi chunk of
 // block kb, [8kb+4, 8kb+8) into its lo chunk -- and then converted in place,
 // block by block, into the augmented bf16 hi/lo row.  Two threads share a
-// row, one per half of the K blocks; a thread only touches its own chunks.
+// row, one per parity of the K blocks (kb = 2j + half); a thread only touches
+// its own chunks.  Blocks wholly beyond the augmented columns (k0 >= d + 2)
+// are cleared once when the kernel starts and never written again.
 template <int KP>
 __device__ __forceinline__ void load_half(__nv_bfloat16* hi, __nv_bfloat16* lo, uint32_t r, uint32_t half,
                                           const float* __restrict__ xr, uint32_t dpad) {
   constexpr int HB = KP / 16;
 #pragma unroll
   for (int j = 0; j < HB; ++j) {
-    const uint32_t kb = half * HB + j, k0 = 8 * kb, off = chunk_off<KP>(r, kb);
+    const uint32_t kb = 2 * j + half, k0 = 8 * kb, off = chunk_off<KP>(r, kb);
     if (k0 < dpad) cp_async16(hi + off, xr + k0);
     if (k0 + 4 < dpad) cp_async16(lo + off, xr + k0 + 4);
   }
@@ -166,9 +169,9 @@ __device__ __forceinline__ void store_split(__nv_bfloat16* hi, __nv_bfloat16* lo
 // accumulated from the scaled values (fma(v, v, acc) = scale^2 fma(t, t, acc')
 // exactly) in K order per half; the halves are added by the caller.
 //
-// Pass 1 writes every K block of this thread except the (at most two)
-// blocks that hold the augmented columns d, d + 1, and returns the partial
-// sum of v^2; pass 2 writes those blocks once the norm is known.  A block
+// Pass 1 writes the K blocks of this thread that hold data columns only,
+// and returns the partial sum of v^2; pass 2 writes the (at most two) blocks
+// that hold the augmented columns d, d + 1 once the norm is known.  A block
 // is read before it is written, so the source may be the destination.
 template <int KP>
 __device__ __forceinline__ float conv_pass1(const __nv_bfloat16* sh, const __nv_bfloat16* sl, __nv_bfloat16* hi,
@@ -176,16 +179,12 @@ __device__ __forceinline__ float conv_pass1(const __nv_bfloat16* sh, const __nv_
                                             float scale, uint32_t d) {
   constexpr int HB = KP / 16;
   float acc = 0.f;
+  if (!ok) return acc;  // a column beyond the tile: its stale values are masked by the epilogue
 #pragma unroll 2
   for (int j = 0; j < HB; ++j) {
-    const uint32_t kb = half * HB + j, k0 = 8 * kb, off = chunk_off<KP>(r, kb);
+    const uint32_t kb = 2 * j + half, k0 = 8 * kb, off = chunk_off<KP>(r, kb);
     float v[8];
-    if (!ok || k0 >= d + 2) {  // zero block
-#pragma unroll
-      for (int i = 0; i < 8; ++i) v[i] = 0.f;
-      store_split(hi, lo, off, v);
-      continue;
-    }
+    if (k0 >= d + 2) continue;  // zero block (cleared at the start)
     float x[8];
     unpack8(sh, sl, off, true, k0 + 4 < d, x);
     if (k0 + 8 <= d) {  // full block
@@ -216,7 +215,7 @@ __device__ __forceinline__ void conv_pass2(const __nv_bfloat16* sh, const __nv_b
   if (!ok) return;
 #pragma unroll 1
   for (int j = 0; j < HB; ++j) {
-    const uint32_t kb = half * HB + j, k0 = 8 * kb, off = chunk_off<KP>(r, kb);
+    const uint32_t kb = 2 * j + half, k0 = 8 * kb, off = chunk_off<KP>(r, kb);
     if (k0 + 8 <= d || k0 >= d + 2) continue;
     float x[8], v[8];
     unpack8(sh, sl, off, k0 < d, k0 + 4 < d, x);
@@ -267,6 +266,12 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&S.tmem_base)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
+  {  // operand buffers start at zero: K blocks beyond the augmented columns are never written
+    uint4* z = reinterpret_cast<uint4*>(tc_dyn);
+    const uint32_t nz = (2 * G + 2 * NS) * OPB * (uint32_t)sizeof(__nv_bfloat16) / 16;
+    for (uint32_t i = tid; i < nz; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
@@ -274,13 +279,25 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
 
   if (warp < NPW) {
     // ============================ producers (NPW warps, two threads per row)
-    // Thread (prow, half): row prow = 16 * warp + lane % 16 of every operand
-    // tile, K blocks [half * KP/16, (half + 1) * KP/16).  Every branch that
+    // Thread (prow, half): row prow = 32 * (warp % 4) + lane of every operand
+    // tile, K blocks kb = 2j + half with half = warp / 4, so the lanes of a
+    // warp take the same branches; the two halves of a row norm meet in
+    // S.npart (one bar.sync).  Every branch that
     // leads to bar.sync is taken on a value all producer threads hold in
     // registers or read from shared memory after the same bar.sync; barrier
     // waits are done by thread 0 and broadcast through S.pflag[2] (two slots:
     // a thread is at most one bar.sync behind thread 0).
-    const uint32_t prow = ((uint32_t)warp << 4) | (lane & 15), half = lane >> 4;
+    const uint32_t prow = ((uint32_t)(warp & 3) << 5) | (uint32_t)lane, half = (uint32_t)warp >> 2;
+    uint32_t xpar = 0;  // parity of the next S.npart exchange
+    // row norm from this thread's part and the other half's (all producer
+    // threads call it together)
+    auto row_norm = [&](float part) {
+      S.npart[xpar][half][prow] = part;
+      prod_sync();
+      const float o = S.npart[xpar][half ^ 1][prow];
+      xpar ^= 1;
+      return half == 0 ? part + o : o + part;  // the same sum, in the same order, in both threads
+    };
     uint32_t tile = 0, issued = 0, unit_k = 0, pf = 0;
     unsigned long long n_tiles = 0, n_cells = 0;
     long long pw_sfree = 0, pc_unit = 0, pc_win = 0, pc_conv = 0, pc_ldw = 0;
@@ -369,7 +386,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
           const bool ok = g * TM + prow < na;
           __nv_bfloat16 *ah = Ahi + g * OPB, *al = Alo + g * OPB;
           const float part = conv_pass1<KP>(ah, al, ah, al, prow, half, ok, S.cadd_a, 1.f, P.d);
-          const float nrm = part + __shfl_xor_sync(FULL_MASK, part, 16);
+          const float nrm = row_norm(part);
           conv_pass2<KP>(ah, al, ah, al, prow, half, ok, S.cadd_a, 1.f, P.d, nrm, 1.f);
           m = fmaxf(m, ok ? nrm : 0.f);
         }
@@ -427,7 +444,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         const uint32_t ncols = min((uint32_t)TN, w_total - w_pos);
         const bool last = (w_pos + TN >= w_total) && (seg_next >= U.s1);
         uint32_t q = 0xffffffffu;
-        if (half == 0 && prow < ncols) {
+        if (prow < ncols) {
           const uint32_t rank = w_pos + prow;
           int lo = 0, hi = (int)w_nb - 1;
           while (lo < hi) {
@@ -436,7 +453,6 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
           }
           q = S.w_start[lo] + (rank - S.w_pref[lo]);
         }
-        q = __shfl_sync(FULL_MASK, q, lane & 15);
         __nv_bfloat16 *dh, *dl;  // landing slot of the raw rows
         uint32_t* iddst;  // candidate ids
         if (RAW > 0) {
@@ -534,7 +550,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         const bool ok = prow < ncols;
         const long long cp0 = T.prof ? clock64() : 0;
         const float part = conv_pass1<KP>(sh, sl, bh, bl, prow, half, ok, S.cadd_b, -2.f, P.d);
-        const float nq2 = (part + __shfl_xor_sync(FULL_MASK, part, 16)) * 0.25f;
+        const float nq2 = row_norm(part) * 0.25f;
         float tcol = 0.f, dl = 0.f;
         if (ok && !column_threshold(tb, ra2max, nq2, &tcol, &dl)) {
           tcol = 1e30f;   // every row of this column becomes a candidate ...
@@ -717,19 +733,19 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         tmem_ld32_nowait(tbase + b * TN + ((quarter * 32u) << 16) + c0, v);
         tmem_wait();
         if (T.prof) ec_ld += clock64() - cl0;
-        uint32_t o = 0;
+        // sign bits (D' < 0: a candidate), column c0 + j at bit j: one
+        // funnel shift per value
+        uint32_t m = 0;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) o |= v[j];
-        uint32_t acc_bits = 0, band_bits = 0;
+        for (int j = 31; j >= 0; --j) m = __funnelshift_l(v[j], m, 1);
         const uint32_t nvalid = min(32u, M.ncols - c0);
-        const bool maybe = row_ok && (o >> 31);
+        if (nvalid < 32) m &= (1u << nvalid) - 1u;
+        if (!row_ok) m = 0;
+        uint32_t acc_bits = 0, band_bits = 0;
+        const bool maybe = m != 0;
         const long long cs0 = T.prof ? clock64() : 0;
         if (__any_sync(FULL_MASK, maybe)) {
           if (maybe) {
-            uint32_t m = 0;
-#pragma unroll
-            for (int j = 0; j < 32; ++j) m |= (v[j] >> 31) << j;
-            m &= nvalid >= 32 ? FULL_MASK : ((1u << nvalid) - 1u);
             // home bin: a pair (a, q) of two home rows is kept only for a < q
             // (sorted positions); the home rows of this tile are the columns
             // [hlo, hhi), column c at position hq + c - hlo

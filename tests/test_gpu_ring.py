@@ -36,7 +36,13 @@ def test_ring_384_dimensional(handle, mode):
     wl = W.tiny384(6000)
     x, eps = wl.pts, wl.eps
     ref = O.brute_pairs(x, eps)
-    r = handle.selfjoin(x, 8, eps, mode=mode, pairs="host", sort_pairs=True, ring_capacity=2048)
+    # a unit holds at most 256 home rows, so no unit has more pairs than the
+    # 256 largest neighbour counts together: a ring of that size always
+    # makes progress, and a ring below the total needs several passes
+    deg = np.bincount(ref.ravel(), minlength=x.shape[0])
+    cap = int(np.sort(deg)[-256:].sum()) + 1
+    assert cap < len(ref)
+    r = handle.selfjoin(x, 8, eps, mode=mode, pairs="host", sort_pairs=True, ring_capacity=cap)
     assert r.n_units_tc > 0 and r.ring_passes > 1
     assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)
 
