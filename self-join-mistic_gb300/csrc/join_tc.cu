@@ -169,14 +169,16 @@ __device__ __forceinline__ void store_split(__nv_bfloat16* hi, __nv_bfloat16* lo
 // accumulated from the scaled values (fma(v, v, acc) = scale^2 fma(t, t, acc')
 // exactly) in K order per half; the halves are added by the caller.
 //
-// Pass 1 writes the K blocks of this thread that hold data columns only,
-// and returns the partial sum of v^2; pass 2 writes the (at most two) blocks
-// that hold the augmented columns d, d + 1 once the norm is known.  A block
-// is read before it is written, so the source may be the destination.
+// Pass 1 writes every K block of this thread that holds a data or an
+// augmented column, with placeholders pd, pd1 in the augmented columns d and
+// d + 1, and returns the partial sum of v^2; once the two halves of the norm
+// are added, patch_col writes the one augmented value that depends on it
+// (|a'|^2 in column d of A, |q'|^2 - T in column d + 1 of B).  A block is
+// read before it is written, so the source may be the destination.
 template <int KP>
 __device__ __forceinline__ float conv_pass1(const __nv_bfloat16* sh, const __nv_bfloat16* sl, __nv_bfloat16* hi,
                                             __nv_bfloat16* lo, uint32_t r, uint32_t half, bool ok, const float* cadd,
-                                            float scale, uint32_t d) {
+                                            float scale, uint32_t d, float pd, float pd1) {
   constexpr int HB = KP / 16;
   float acc = 0.f;
   if (!ok) return acc;  // a column beyond the tile: its stale values are masked by the epilogue
@@ -186,50 +188,41 @@ __device__ __forceinline__ float conv_pass1(const __nv_bfloat16* sh, const __nv_
     float v[8];
     if (k0 >= d + 2) continue;  // zero block (cleared at the start)
     float x[8];
-    unpack8(sh, sl, off, true, k0 + 4 < d, x);
+    unpack8(sh, sl, off, k0 < d, k0 + 4 < d, x);
     if (k0 + 8 <= d) {  // full block
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         v[i] = fmaf(x[i], scale, cadd[k0 + i]);
         acc = fmaf(v[i], v[i], acc);
       }
-      store_split(hi, lo, off, v);
-    } else {  // holds d or d + 1: norm part only
+    } else {  // holds d or d + 1
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        if (k0 + i < d) {
-          const float t = fmaf(x[i], scale, cadd[k0 + i]);
+        const uint32_t k = k0 + i;
+        float t = 0.f;
+        if (k < d) {
+          t = fmaf(x[i], scale, cadd[k]);
           acc = fmaf(t, t, acc);
+        } else if (k == d) {
+          t = pd;
+        } else if (k == d + 1) {
+          t = pd1;
         }
+        v[i] = t;
       }
     }
+    store_split(hi, lo, off, v);
   }
   return acc;
 }
 
+// Column k of row r := v, split into bf16 hi + lo as store_split does.
 template <int KP>
-__device__ __forceinline__ void conv_pass2(const __nv_bfloat16* sh, const __nv_bfloat16* sl, __nv_bfloat16* hi,
-                                           __nv_bfloat16* lo, uint32_t r, uint32_t half, bool ok, const float* cadd,
-                                           float scale, uint32_t d, float e_d, float e_d1) {
-  constexpr int HB = KP / 16;
-  if (!ok) return;
-#pragma unroll 1
-  for (int j = 0; j < HB; ++j) {
-    const uint32_t kb = 2 * j + half, k0 = 8 * kb, off = chunk_off<KP>(r, kb);
-    if (k0 + 8 <= d || k0 >= d + 2) continue;
-    float x[8], v[8];
-    unpack8(sh, sl, off, k0 < d, k0 + 4 < d, x);
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const uint32_t k = k0 + i;
-      float t = 0.f;
-      if (k < d) t = fmaf(x[i], scale, cadd[k]);
-      if (k == d) t = e_d;
-      if (k == d + 1) t = e_d1;
-      v[i] = t;
-    }
-    store_split(hi, lo, off, v);
-  }
+__device__ __forceinline__ void patch_col(__nv_bfloat16* hi, __nv_bfloat16* lo, uint32_t r, uint32_t k, float v) {
+  const uint32_t off = chunk_off<KP>(r, k >> 3) + (k & 7);
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  hi[off] = h;
+  lo[off] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
 template <int KP, int NS, int G, int RAW, int NEPI>
@@ -385,9 +378,9 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         for (uint32_t g = 0; g < ng; ++g) {
           const bool ok = g * TM + prow < na;
           __nv_bfloat16 *ah = Ahi + g * OPB, *al = Alo + g * OPB;
-          const float part = conv_pass1<KP>(ah, al, ah, al, prow, half, ok, S.cadd_a, 1.f, P.d);
+          const float part = conv_pass1<KP>(ah, al, ah, al, prow, half, ok, S.cadd_a, 1.f, P.d, 0.f, 1.f);
           const float nrm = row_norm(part);
-          conv_pass2<KP>(ah, al, ah, al, prow, half, ok, S.cadd_a, 1.f, P.d, nrm, 1.f);
+          if (ok && ((P.d >> 3) & 1u) == half) patch_col<KP>(ah, al, prow, P.d, nrm);
           m = fmaxf(m, ok ? nrm : 0.f);
         }
 #pragma unroll
@@ -443,15 +436,25 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         const long long ca0 = T.prof ? clock64() : 0;
         const uint32_t ncols = min((uint32_t)TN, w_total - w_pos);
         const bool last = (w_pos + TN >= w_total) && (seg_next >= U.s1);
+        // row of candidate rank w_pos + prow: the warp finds the bin of its
+        // first rank (two 32-way probes of the window prefix), then each lane
+        // counts the bin boundaries among the next 32 ranks
         uint32_t q = 0xffffffffu;
-        if (prow < ncols) {
-          const uint32_t rank = w_pos + prow;
-          int lo = 0, hi = (int)w_nb - 1;
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (S.w_pref[mid] <= rank) lo = mid; else hi = mid - 1;
+        {
+          const uint32_t r0 = w_pos + (prow & ~31u);
+          const uint32_t step = (w_nb + 31) >> 5;
+          const uint32_t c = __popc(__ballot_sync(FULL_MASK, lane * step < w_nb && S.w_pref[lane * step] <= r0));
+          const uint32_t base = (c - 1) * step;  // w_pref[0] = 0 <= r0, so c >= 1
+          const uint32_t b0 =
+              base + __popc(__ballot_sync(FULL_MASK, (uint32_t)lane < step && base + lane < w_nb &&
+                                                         S.w_pref[base + lane] <= r0)) - 1;
+          const uint32_t e = b0 + 1 + lane;  // boundary after bin b0 + lane
+          const uint32_t t = e <= w_nb ? S.w_pref[e] - r0 : 32u;
+          const uint32_t bounds = __reduce_or_sync(FULL_MASK, t < 32u ? 1u << t : 0u);
+          if (prow < ncols) {
+            const uint32_t b = b0 + __popc(bounds & ((2u << lane) - 1u));
+            q = S.w_start[b] + (r0 + lane - S.w_pref[b]);
           }
-          q = S.w_start[lo] + (rank - S.w_pref[lo]);
         }
         __nv_bfloat16 *dh, *dl;  // landing slot of the raw rows
         uint32_t* iddst;  // candidate ids
@@ -549,7 +552,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         }
         const bool ok = prow < ncols;
         const long long cp0 = T.prof ? clock64() : 0;
-        const float part = conv_pass1<KP>(sh, sl, bh, bl, prow, half, ok, S.cadd_b, -2.f, P.d);
+        const float part = conv_pass1<KP>(sh, sl, bh, bl, prow, half, ok, S.cadd_b, -2.f, P.d, 1.f, 0.f);
         const float nq2 = row_norm(part) * 0.25f;
         float tcol = 0.f, dl = 0.f;
         if (ok && !column_threshold(tb, ra2max, nq2, &tcol, &dl)) {
@@ -557,7 +560,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
           dl = INFINITY;  // ... and none is accepted without the FP64 check
         }
         const long long cp1 = T.prof ? clock64() : 0;
-        conv_pass2<KP>(sh, sl, bh, bl, prow, half, ok, S.cadd_b, -2.f, P.d, 1.f, nq2 - tcol);
+        if (ok && (((P.d + 1) >> 3) & 1u) == half) patch_col<KP>(bh, bl, prow, P.d + 1, nq2 - tcol);
         const long long cp2 = T.prof ? clock64() : 0;
         if (T.prof) {
           pc_p1 += cp1 - cp0;

@@ -323,10 +323,12 @@ int bit_length(uint64_t v) {
 uint32_t tc_min_bin(uint32_t d, bool wide) {
   const char* e = getenv("MISTIC_TC_MIN_BIN");
   if (e && *e) return (uint32_t)std::max(1l, strtol(e, nullptr, 10));
-  // long rows (K-chunked kernel): a tile costs ~3 * 2 * 128 * d tensor flops
-  // per candidate column whatever its home rows, the FP32 CUDA cores 3 d per
-  // row and column; measured on 2M x 384: T = 8: 1383, 16: 1422, 24: 1514 ms
-  if (wide) return 8;
+  // long rows (K-chunked kernel): every bin.  Even a one-row bin is joined
+  // faster on the tensor cores (a 128-row tile at ~1/128 use) than by the
+  // FP32 CUDA-core kernel, whose units of a small home bin against a very
+  // large neighbour bin (one segment holds a whole bin) run on single warps:
+  // on the 5M x 384 workload such units took 2.1 s of a 14 s join at T = 8.
+  if (wide) return 1;
   return (uint32_t)std::min(96.0, std::max(1.0, std::floor(29000.0 / ((double)d * d))));
 }
 
@@ -494,15 +496,14 @@ bool tune_lookup(mistic_handle_s* h, const mistic_opts& o, uint32_t d, mistic_dt
   }
   const int eps_cls = (eps2 > 0 && R > 0) ? (int)std::floor(std::log2(R * R / eps2)) : 0;
   char key[160];
-  snprintf(key, sizeof key, "v2 d=%u dt=%d %s bins=%d,%d r2e=%d", d, (int)dt, wide ? "tcw" : "tc", c50, c90, eps_cls);
+  snprintf(key, sizeof key, "v3 d=%u dt=%d %s bins=%d,%d r2e=%d", d, (int)dt, wide ? "tcw" : "tc", c50, c90, eps_cls);
   if (tune_cache().find(key, out)) return true;
   // candidates
   std::vector<TuneCandidate> cands;
   if (wide) {
     std::vector<int> precs = {0};
     if (prec_default == 1) precs.push_back(1);  // single bf16 only where its bound fits the cap
-    for (int pr : precs)
-      for (uint32_t t : {1u, 8u}) cands.push_back({t, pr});
+    for (int pr : precs) cands.push_back({1u, pr});  // every bin on the tensor cores (see tc_min_bin)
   } else {
     const uint32_t t0 = tc_min_bin(d, false);
     for (uint32_t t : {std::max(1u, t0 / 2), t0, std::min(512u, 2 * t0)})

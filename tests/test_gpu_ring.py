@@ -33,16 +33,18 @@ def test_ring_low_dimensional_sample(handle, mode):
 
 @pytest.mark.parametrize("mode", ["bf16", "tf32"])
 def test_ring_384_dimensional(handle, mode):
-    wl = W.tiny384(6000)
-    x, eps = wl.pts, wl.eps
+    """Long rows on the K-chunked tensor-core kernel: 3,000 pairs of near
+    duplicates among unit-norm 384-d rows, so a unit (at most 256 home rows,
+    one neighbour each) never holds more than 256 pairs and a ring of 512
+    needs several passes."""
+    rng = np.random.default_rng(46)
+    x = rng.normal(size=(6000, 384)).astype(np.float32)
+    x /= np.linalg.norm(x, axis=1, keepdims=True)
+    x[3000:] = x[:3000] + rng.normal(scale=0.01, size=(3000, 384)).astype(np.float32)
+    eps = 0.3
     ref = O.brute_pairs(x, eps)
-    # a unit holds at most 256 home rows, so no unit has more pairs than the
-    # 256 largest neighbour counts together: a ring of that size always
-    # makes progress, and a ring below the total needs several passes
-    deg = np.bincount(ref.ravel(), minlength=x.shape[0])
-    cap = int(np.sort(deg)[-256:].sum()) + 1
-    assert cap < len(ref)
-    r = handle.selfjoin(x, 8, eps, mode=mode, pairs="host", sort_pairs=True, ring_capacity=cap)
+    assert len(ref) == 3000
+    r = handle.selfjoin(x, 8, eps, mode=mode, pairs="host", sort_pairs=True, ring_capacity=512)
     assert r.n_units_tc > 0 and r.ring_passes > 1
     assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)
 
