@@ -185,6 +185,29 @@ def cpu_sample(x: np.ndarray, eps: float, seconds: float) -> dict:
             "points_per_s": n / job_s, "evals_per_s": rows * n / t}
 
 
+def host_join_sample(x: np.ndarray, eps: float, k: int, seconds: float) -> dict:
+    """The project's own indexed host join (oracle/hostjoin.c: the same
+    reference-point bins, FP64 predicate, OpenMP on all host threads).  The
+    index build and the neighbour enumeration run in full; the distance work
+    runs on every S-th home bin, S chosen so that it takes about `seconds`,
+    and is scaled to the whole join by candidate pairs."""
+    from oracle import oracle as O
+    threads = O.max_threads()
+    rp = O.pca_far_points(x, k)
+    probe = O.host_join(x, eps, rp, home_stride=4096, threads=threads)
+    per_cand = probe["s_join"] / max(1, probe["cand_sampled"])
+    full_join = per_cand * probe["cand_all"]
+    stride = max(1, int(math.ceil(full_join / max(seconds, 1e-3)))) if probe["cand_sampled"] else 4096
+    r = O.host_join(x, eps, rp, home_stride=stride, threads=threads)
+    join_s = r["s_join"] * r["cand_all"] / max(1, r["cand_sampled"])
+    job_s = r["s_index"] + join_s
+    return {"value": x.shape[0] / job_s, "unit": UNIT, "cores": threads, "kind": "project host join",
+            "job_seconds": job_s, "index_and_enumeration_s": r["s_index"], "join_s_extrapolated": join_s,
+            "sample": f"every {stride}-th of {r['bins']} home bins joined ({r['s_join']:.1f} s, "
+                      f"{r['cand_sampled']} of {r['cand_all']} candidate pairs), scaled by candidate pairs",
+            "evals_per_s": r["cand_sampled"] / max(r["s_join"], 1e-9)}
+
+
 # ------------------------------------------------------------------ arms
 def dist_env():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
@@ -414,6 +437,7 @@ def run_mistic(args, wl) -> None:
     step_roof = step_lower_bound(r, n, d, wl.k, ms, peaks)
     north = None if (args.no_c5 or args.workload == "tiny384") else run_north_star(h, args, dev, stream, peaks)
     cpu = cpu_sample(x, wl.eps, args.cpu_seconds) if not args.no_cpu else None
+    host = host_join_sample(x, wl.eps, wl.k, args.cpu_seconds) if not args.no_cpu else None
     ref_gpu = reference_gpu(x, wl.k, wl.eps, r.pairs_ordered_incl_self, args.ref_gpu_timeout) \
         if args.ref_gpu else None
     value = job_points_per_s(n, world, ms)
@@ -447,6 +471,7 @@ def run_mistic(args, wl) -> None:
             "sample": f"rows [0,{cpu['rows']}) x all {n} rows ({cpu['seconds']:.1f} s), extrapolated to "
                       f"n rows; brute_force of src/utils.cu:285-317 (oracle C port, OpenMP)",
             "evals_per_s": cpu["evals_per_s"]},
+        "cpu_host_join": host,
     }
     print(json.dumps(line), flush=True)
     h.close()

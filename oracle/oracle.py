@@ -20,8 +20,8 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile liboracle.so with the committed Makefile (gcc, no GPU)."""
-    src = os.path.join(_HERE, "brute.c")
-    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("brute.c", "hostjoin.c", "Makefile")]
+    if force or not os.path.exists(_LIB) or any(os.path.getmtime(_LIB) < os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
     return _LIB
 
@@ -47,6 +47,10 @@ def lib():
         L.oracle_sqdist.restype = dbl
         L.oracle_sqdist.argtypes = [vp, i32, u64, u64, u32]
         L.oracle_max_threads.restype = i32
+        L.hostjoin_count.restype = u64
+        L.hostjoin_count.argtypes = [vp, u64, u32, vp, i32, dbl, u64, i32, ctypes.POINTER(u64),
+                                     ctypes.POINTER(u64), ctypes.POINTER(dbl), ctypes.POINTER(dbl),
+                                     ctypes.POINTER(u64)]
         L.oracle_free.argtypes = [vp]
         _lib = L
     return _lib
@@ -118,3 +122,34 @@ def sqdist(pts: np.ndarray, i: int, j: int) -> float:
 
 def max_threads() -> int:
     return int(lib().oracle_max_threads())
+
+
+def pca_far_points(pts: np.ndarray, k: int, sample: int = 8192, seed: int = 0) -> np.ndarray:
+    """k reference points for the host grid join: the sample mean moved well
+    outside the data along the sample's top-k principal axes (far points make
+    the distance fields nearly linear projections)."""
+    x = np.asarray(pts, dtype=np.float64)
+    rng = np.random.default_rng(seed)
+    s = x[rng.choice(x.shape[0], size=min(sample, x.shape[0]), replace=False)] if x.shape[0] > sample else x
+    mu = s.mean(axis=0)
+    c = s - mu
+    _, _, vt = np.linalg.svd(c, full_matrices=False)
+    span = float(np.max(np.linalg.norm(c, axis=1))) if c.size else 1.0
+    k = min(k, vt.shape[0])
+    return np.ascontiguousarray(mu + 10.0 * max(span, 1e-300) * vt[:k], dtype=np.float64)
+
+
+def host_join(pts: np.ndarray, eps: float, rps: np.ndarray, home_stride: int = 1, threads: int = 0) -> dict:
+    """The project's own OpenMP host grid join (oracle/hostjoin.c): unordered
+    pairs of the joined home bins (every `home_stride`-th), their candidate
+    pairs and those of all bins, and the seconds of the index build with the
+    neighbour enumeration and of the sampled distance work."""
+    x = np.ascontiguousarray(pts, dtype=np.float64)
+    r = np.ascontiguousarray(rps, dtype=np.float64)
+    cs, ca, nb = ctypes.c_uint64(0), ctypes.c_uint64(0), ctypes.c_uint64(0)
+    si, sj = ctypes.c_double(0), ctypes.c_double(0)
+    p = lib().hostjoin_count(x.ctypes.data, x.shape[0], x.shape[1], r.ctypes.data, r.shape[0], float(eps),
+                             int(home_stride), threads, ctypes.byref(cs), ctypes.byref(ca), ctypes.byref(si),
+                             ctypes.byref(sj), ctypes.byref(nb))
+    return {"pairs": int(p), "cand_sampled": int(cs.value), "cand_all": int(ca.value), "s_index": si.value,
+            "s_join": sj.value, "bins": int(nb.value)}
