@@ -7,9 +7,11 @@
 # "Total results Set Size" is compared with the oracle's count; nothing of it
 # enters the library.
 #
-# The reference hard-codes CUDA_DEVICE 1 (include/params.cuh:40) and never
-# checks cudaSetDevice's status, so on a one-GPU machine its calls stay on
-# device 0 without a patch.
+# The reference hard-codes CUDA_DEVICE 1 (include/params.cuh:40); on a
+# one-GPU machine cudaSetDevice(1) fails and thrust then reports "invalid
+# device ordinal".  The sources are compiled with cudaSetDevice renamed to
+# mistic_ref_set_device (oracle/ref_device_shim.cpp), which selects device 0;
+# no source line is changed.
 #
 # The GPU machines have no reference tree and run no binary built here, so
 # where the tree is present (argument 1, $MISTIC_REFERENCE_ROOT, or a checkout
@@ -37,7 +39,7 @@ if [ ! -f "$SRC/src/launcher.cu" ]; then
   exit 0
 fi
 command -v nvcc >/dev/null || { echo "nvcc not found" >&2; exit 1; }
-FLAGS="-O3 -gencode arch=compute_103a,code=sm_103a -Xcompiler -fopenmp -DBS=256 -DKB=1024 -I$SRC"
+FLAGS="-O3 -gencode arch=compute_103a,code=sm_103a -Xcompiler -fopenmp -DBS=256 -DKB=1024 -I$SRC -DcudaSetDevice=mistic_ref_set_device"
 for D in $DIMS; do
   B="$OUT/build_d$D"
   mkdir -p "$B"
@@ -46,6 +48,8 @@ for D in $DIMS; do
     nvcc $FLAGS -DDIM="$D" -c "$SRC/src/$f.cu" -o "$B/$f.o" > "$B/$f.log" 2>&1 &
     pids+=($!)
   done
+  nvcc -O2 -c "$HERE/ref_device_shim.cpp" -o "$B/shim.o" &
+  pids+=($!)
   for p in "${pids[@]}"; do wait "$p"; done
   nvcc -gencode arch=compute_103a,code=sm_103a -Xcompiler -fopenmp "$B"/*.o -o "$OUT/ref_main_d$D" -lcuda
   echo "built $OUT/ref_main_d$D"

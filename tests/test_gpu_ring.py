@@ -51,8 +51,9 @@ def test_ring_384_dimensional(handle, mode):
 
 def test_ring_to_a_host_sink(handle):
     x = np.random.default_rng(45).random((30000, 8))
-    eps = 0.11
+    eps = 0.3
     ref = O.brute_pairs(x, eps)
+    assert len(ref) > 10 * 3000
     got = []
     SINK = ctypes.CFUNCTYPE(None, ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint64, ctypes.c_void_p)
 
