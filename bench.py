@@ -407,9 +407,11 @@ def run_mistic(args, wl) -> None:
         # evaluated (home row, candidate) cell, one contraction of length d
         work = r.tc_cells * 2.0 * d
         achieved = work / (tc_ms * 1e-3) / 1e12
-        wide = (d + 2 + 15) // 16 * 16 > 128  # K-chunked long-row kernel
+        wide = r.tc_kernel == "k-chunked"  # rows prepared once (long rows, or medium rows whose bound allows)
         kname = "k_join_tcw" if wide else "k_join_tc"
-        kmma = ((d + 31) // 32 * 32) if wide else (d + 2 + 15) // 16 * 16
+        kstage = 64 if r.tc_operands == "bf16" else 32
+        kmma = ((d + kstage - 1) // kstage * kstage) if wide else (d + 2 + 15) // 16 * 16
+        nprod = 3 if r.tc_operands == "split-bf16" else 1
         roof = {"bound": "tensor", "kernel": kname, "achieved": achieved,
                 "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
                 "frac": achieved / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
@@ -418,7 +420,10 @@ def run_mistic(args, wl) -> None:
                 "cells": r.tc_cells, "fp32_simt_peak_tflops": fp32_peak,
                 # tensor-pipe work actually issued: 3 split products x 2 * K per
                 # 128 x 128 tile cell (padding and empty rows/columns included)
-                "issued_tflops": r.tc_tiles * 128 * 128 * 3 * 2.0 * kmma / (tc_ms * 1e-3) / 1e12}
+                # (K-chunked kernel: tiles count 128 x 128 MMA tiles; the short-row
+                # kernel counts candidate tiles, each issued once per home chunk)
+                "issued_tflops": (r.tc_tiles * 128 * 128 * nprod * 2.0 * kmma / (tc_ms * 1e-3) / 1e12)
+                if wide else None}
         if args.workload == "susy18":
             roof["traffic"] = TC_DRAM_BYTES_PER_CELL_SUSY18 * r.tc_cells
             roof["traffic_source"] = ("ncu dram__bytes_read+write per cell of a 2.5M-point capture of the "
@@ -446,7 +451,8 @@ def run_mistic(args, wl) -> None:
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_for(args, wl, world),
-        "mode_used": r.mode_used, "tc_operands": r.tc_operands,
+        "mode_used": r.mode_used, "tc_operands": r.tc_operands, "tc_kernel": r.tc_kernel,
+        "tc_min_bin": r.tc_min_bin, "tuned": r.tuned,
         "pairs_ij": r.pairs_ij, "pairs_ordered_incl_self": r.pairs_ordered_incl_self,
         "candidates": r.candidates, "band_pairs": r.band_pairs, "ulp_ambiguous": r.ulp_ambiguous,
         "band_fraction": r.band_pairs / max(1, r.candidates),
@@ -608,7 +614,8 @@ def run_north_star(h, args, dev, stream, peaks) -> dict:
         "workload": "tiny384", "n": n, "d": d, "k": wl.k, "eps_hex": float(wl.eps).hex(),
         "desc": WORKLOADS["tiny384"][1], "generation_s": gen_s,
         "steps": args.c5_steps, "warmup": 1, "ms_per_step": ms, "value": n / (ms * 1e-3), "unit": UNIT,
-        "mode_used": r.mode_used, "tc_operands": r.tc_operands,
+        "mode_used": r.mode_used, "tc_operands": r.tc_operands, "tc_kernel": r.tc_kernel,
+        "tc_min_bin": r.tc_min_bin, "tuned": r.tuned,
         "pairs_ij": r.pairs_ij, "candidates": r.candidates, "band_pairs": r.band_pairs,
         "band_fraction": r.band_pairs / max(1, r.candidates), "ulp_ambiguous": r.ulp_ambiguous,
         "distance_evals_per_s": r.candidates / (ms * 1e-3), "pairs_per_s": r.pairs_ij / (ms * 1e-3),

@@ -46,7 +46,7 @@
 extern "C" {
 #endif
 
-#define MISTIC_ABI_VERSION 1
+#define MISTIC_ABI_VERSION 2
 
 typedef enum mistic_status {
   MISTIC_OK = 0,
@@ -187,6 +187,9 @@ typedef struct mistic_result {
                                        (measured now, or cached for this shape) */
   uint32_t ring_passes;             /* ring mode: join passes (ring drains) */
   uint64_t ring_units_redone;       /* ring mode: units run again after the ring filled */
+  int32_t tc_kernel;                /* tensor-core join used: 0 none, 1 short rows (per-unit
+                                       centred operands converted per tile), 2 K-chunked (rows
+                                       prepared once, globally centred) */
   void* _owner;                     /* internal: non-NULL when the result owns `pairs` */
 } mistic_result;
 

@@ -373,6 +373,25 @@ int tc_precision(mistic_mode mode, uint32_t d, double eps2, double R) {
   return E <= 0.1 * eps2 ? 1 : 0;
 }
 
+// Rows of 32 < d <= 126 on the K-chunked kernel too, when its globally
+// centred bound keeps the band narrow: split-bf16 error for the widest
+// columns (rows at the largest norm R) at most eps^2 / 100.  The short-row
+// kernel centres each unit on its first row, which keeps the bound small
+// whatever the coordinates, but converts every candidate tile on its CUDA
+// cores; the K-chunked kernel reads rows prepared once.  On the 515k x 90
+// workload (eps^2 = 50, R ~ 15) the short-row kernel was latency-bound on
+// that conversion (issue 28 %, tensor pipe 14 %, 237 ms).  MISTIC_TC_WIDE=0/1
+// overrides.
+bool tcw_for_medium_rows(uint32_t d, double eps2, double R) {
+  if (const char* e = getenv("MISTIC_TC_WIDE")) return *e == '1';
+  if (d <= 32) return false;
+  const double u = ldexp(1.0, -24);
+  const double rs = 2.0 * R, Dp = 1.1 * sqrt(eps2);
+  const double delta = 2.0 * u * R + u * rs;
+  const double E = tc_kappa(d, true, 0) * (rs * rs + 1.2 * eps2) + delta * (2.0 * Dp + delta);
+  return E <= 0.01 * eps2;
+}
+
 void check_handle(mistic_handle h) {
   if (!h) throw Error(MISTIC_ERR_INVALID_ARG, "null handle");
   MCK(cudaSetDevice(h->device));
@@ -839,7 +858,8 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   // long rows (augmented K above one 128-wide operand tile), and every row in
   // tf32 mode, use the K-chunked kernel over rows prepared once; its operand
   // precision is picked from the bound (see tc_precision)
-  const bool wide = use_tc && (tf32_mode || join::tc_kp(d) > 128);
+  // (the fused batch join drains medium rows with the short-row kernel only)
+  const bool wide = use_tc && (tf32_mode || join::tc_kp(d) > 128 || (!ex && tcw_for_medium_rows(d, eps2, R)));
   const int prec = wide ? tc_precision(o.mode, d, eps2, R) : 0;
   r->mode_used = fp64 ? MISTIC_MODE_FP64
                       : (use_tc ? (tf32_mode ? MISTIC_MODE_TF32 : MISTIC_MODE_BF16) : MISTIC_MODE_FP32);
@@ -1118,6 +1138,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
       ex->CH = CH;
       ex->exported = true;
       r->tc_operands = (use_tc && tots[2] > 0) ? 1 : 0;
+      r->tc_kernel = (use_tc && tots[2] > 0) ? 1 : 0;
       MCK(cudaStreamSynchronize(h->stream));  // the arena is reused by this handle's next call
       r->ms_wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
       r->kernel_launches = h->launches - launches0;
@@ -1281,6 +1302,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     r->ring_passes = passes;
     r->ring_units_redone = redone;
     r->tc_operands = (use_tc && tots[2] > 0) ? (wide ? 1 + prec_used : 1) : 0;
+    r->tc_kernel = (use_tc && tots[2] > 0) ? (wide ? 2 : 1) : 0;
     if (!o.pair_sink) {
       if (o.sort_pairs) std::sort(all.begin(), all.end());
       uint32_t* hp = (uint32_t*)pinned_cache().acquire(std::max<size_t>(1, all.size() * 8));
@@ -1363,6 +1385,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   r->band_pairs = fp64 ? 0 : hc.band;
   r->ulp_ambiguous = hc.ambiguous;
   r->tc_operands = (use_tc && tots[2] > 0) ? (wide ? 1 + prec_used : 1) : 0;
+  r->tc_kernel = (use_tc && tots[2] > 0) ? (wide ? 2 : 1) : 0;
   if (use_tc) {
     JoinCounters tcc{};
     d2h(h, &tcc, ctr + 1, sizeof tcc);

@@ -58,6 +58,7 @@ class JoinResult:
     tuned: bool = False                      # threshold / operands from the autotuner
     ring_passes: int = 0                     # ring mode: join passes
     ring_units_redone: int = 0               # ring mode: units run again after the ring filled
+    tc_kernel: str = "none"                  # tensor-core join: none, short-rows, k-chunked
     extra: dict = field(default_factory=dict)
 
 
@@ -162,7 +163,8 @@ class Handle:
             csr_offsets=csr_off, csr_nbrs=csr_nb,
             tc_operands={0: "none", 1: "split-bf16", 2: "bf16", 3: "tf32"}.get(r.tc_operands, "?"),
             tc_min_bin=r.tc_min_bin, tuned=bool(r.tuned), ring_passes=r.ring_passes,
-            ring_units_redone=r.ring_units_redone)
+            ring_units_redone=r.ring_units_redone,
+            tc_kernel={0: "none", 1: "short-rows", 2: "k-chunked"}.get(r.tc_kernel, "?"))
         if not keep_device or not r.pairs_on_device:
             self.lib.mistic_result_free(ctypes.byref(r))
         else:

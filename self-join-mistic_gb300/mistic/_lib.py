@@ -94,6 +94,7 @@ class Result(ctypes.Structure):
         ("tuned", i32),
         ("ring_passes", u32),
         ("ring_units_redone", u64),
+        ("tc_kernel", i32),
         ("_owner", vp),
     ]
 

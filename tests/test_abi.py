@@ -30,7 +30,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version_and_opts_layout():
     lib = L.load()
-    assert lib.mistic_abi_version() == 1
+    assert lib.mistic_abi_version() == 2
     o = L.Opts()
     lib.mistic_opts_init(ctypes.byref(o))
     assert o.struct_size == ctypes.sizeof(L.Opts)

@@ -11,7 +11,7 @@ band to well outside it -- and place them far from the unit's centring row
 (|a'| + |q'| up to the size where E reaches the 0.1 eps^2 cap, beyond which a
 column is decided entirely in FP64).  Every pair set must equal the
 oracle's bit for bit, for the short-row kernel (d = 18, 90) and the K-chunked
-long-row kernel (d = 384).
+kernel (d = 384, and d = 90 routed to it).
 """
 import numpy as np
 import pytest
@@ -62,6 +62,7 @@ def test_pairs_around_the_band(handle, monkeypatch, d, rho_max, prec):
     if prec == "bf16" and d != 384:
         pytest.skip("single bf16 operands exist on the K-chunked kernel only")
     monkeypatch.setenv("MISTIC_TC_MIN_BIN", "1")  # every home bin on the tensor cores
+    monkeypatch.setenv("MISTIC_TC_WIDE", "0")    # d = 90 on the short-row kernel
     if prec == "bf16":
         monkeypatch.setenv("MISTIC_TC_PREC", "bf16")
     x, rps = shell_case(d, 1500, rho_max, seed=d * 100 + int(rho_max))
@@ -71,4 +72,17 @@ def test_pairs_around_the_band(handle, monkeypatch, d, rho_max, prec):
                         pairs="host", sort_pairs=True)
     assert r.n_units_tc > 0 and r.tc_tiles > 0
     assert r.band_pairs > 0
+    assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)
+
+
+@pytest.mark.parametrize("rho_max", [4.0, 12.0])
+def test_pairs_around_the_band_medium_rows_on_the_k_chunked_kernel(handle, monkeypatch, rho_max):
+    """d = 90 on the K-chunked kernel (globally centred rows, prepared once):
+    the same shells around eps^2, pair sets bit-identical to the oracle's."""
+    monkeypatch.setenv("MISTIC_TC_MIN_BIN", "1")
+    monkeypatch.setenv("MISTIC_TC_WIDE", "1")
+    x, rps = shell_case(90, 1500, rho_max, seed=9000 + int(rho_max))
+    ref = O.brute_pairs(x, 1.0)
+    r = handle.selfjoin(x, 2, 1.0, mode="bf16", rp="user", rp_user=rps, pairs="host", sort_pairs=True)
+    assert r.n_units_tc > 0 and r.tc_tiles > 0
     assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)
