@@ -112,7 +112,9 @@ struct TcShared2 {
   uint32_t abort_flag;
   uint32_t tmem_base;
   uint32_t pflag[2];  // producer-wide decisions, written by producer thread 0
-  float npart[2][2][TM];  // [tile parity][K-block parity][row]: partial row norms of the two threads of a row
+  // [tile parity][K-block parity][row]: partial row norms of the two threads
+  // of a row (two-threads-a-row mode only; pair mode has one thread a row)
+  float npart[RAW == 4 ? 1 : 2][2][RAW == 4 ? 1 : TM];
   unsigned long long full[NS], sfree[NS], dfull[NACC], dfree[NACC], afull, afree;
 };
 
@@ -216,6 +218,60 @@ __device__ __forceinline__ float conv_pass1(const __nv_bfloat16* sh, const __nv_
   return acc;
 }
 
+// Whole-row forms for one thread a row (pair mode): the raw row's chunks
+// land in the row's own slots as in load_half, every K block of the row.
+template <int KP>
+__device__ __forceinline__ void load_row(__nv_bfloat16* hi, __nv_bfloat16* lo, uint32_t r,
+                                         const float* __restrict__ xr, uint32_t dpad) {
+#pragma unroll
+  for (int kb = 0; kb < KP / 8; ++kb) {
+    const uint32_t k0 = 8 * kb, off = chunk_off<KP>(r, kb);
+    if (k0 < dpad) cp_async16(hi + off, xr + k0);
+    if (k0 + 4 < dpad) cp_async16(lo + off, xr + k0 + 4);
+  }
+}
+
+// Converts row r from the raw chunks (sh, sl) into the bf16 hi/lo operand row
+// (hi, lo), K blocks in order, with placeholders pd, pd1 in the augmented
+// columns d and d + 1; returns the row norm |x - c|^2 (times scale^2).
+template <int KP>
+__device__ __forceinline__ float conv_row(const __nv_bfloat16* sh, const __nv_bfloat16* sl, __nv_bfloat16* hi,
+                                          __nv_bfloat16* lo, uint32_t r, const float* cadd, float scale, uint32_t d,
+                                          float pd, float pd1) {
+  float acc = 0.f;
+#pragma unroll
+  for (int kb = 0; kb < KP / 8; ++kb) {
+    const uint32_t k0 = 8 * kb, off = chunk_off<KP>(r, kb);
+    if (k0 >= d + 2) break;  // zero blocks (cleared at the start)
+    float x[8], v[8];
+    unpack8(sh, sl, off, k0 < d, k0 + 4 < d, x);
+    if (k0 + 8 <= d) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        v[i] = fmaf(x[i], scale, cadd[k0 + i]);
+        acc = fmaf(v[i], v[i], acc);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const uint32_t k = k0 + i;
+        float t = 0.f;
+        if (k < d) {
+          t = fmaf(x[i], scale, cadd[k]);
+          acc = fmaf(t, t, acc);
+        } else if (k == d) {
+          t = pd;
+        } else if (k == d + 1) {
+          t = pd1;
+        }
+        v[i] = t;
+      }
+    }
+    store_split(hi, lo, off, v);
+  }
+  return acc;
+}
+
 // Column k of row r := v, split into bf16 hi + lo as store_split does.
 template <int KP>
 __device__ __forceinline__ void patch_col(__nv_bfloat16* hi, __nv_bfloat16* lo, uint32_t r, uint32_t k, float v) {
@@ -242,7 +298,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
 
   if (tid == 0) {
     for (int i = 0; i < NS; ++i) {
-      mbar_init(&S.full[i], NPROD);
+      mbar_init(&S.full[i], RAW == 4 ? TM : NPROD);  // pair mode: one group of 128 a tile
       mbar_init(&S.sfree[i], NEPI);
     }
     for (int i = 0; i < NACC; ++i) {
@@ -271,6 +327,321 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
   const uint32_t tbase = S.tmem_base;
 
   if (warp < NPW) {
+    if constexpr (RAW == 4) {
+    // ============================ producers, pair mode (K <= 32, four raw slots)
+    // The 256 producer threads are two groups of 128; thread (grp, pr)
+    // converts the whole row pr of one candidate tile, group grp of each
+    // pair of consecutive tiles, so a row needs no exchange and its fixed
+    // costs (finding its source row, issuing its copies, its threshold and
+    // metadata) are paid once.  Pairs never span a window of neighbour bins:
+    // when fewer than 129 candidate ranks are left in it, the pair is one
+    // tile and group 1 idles.  Up to two pairs are in flight (one raw slot a
+    // tile).  Branches that lead to bar.sync depend only on values every
+    // producer thread holds or reads after the same bar.sync; barrier waits
+    // are done by thread 0 and broadcast through S.pflag.
+    const uint32_t pr = (uint32_t)tid & 127u, grp = (uint32_t)tid >> 7;
+    uint32_t tile = 0, issued = 0, unit_k = 0, pf = 0;
+    unsigned long long n_tiles = 0, n_cells = 0;
+    long long pw_sfree = 0, pc_unit = 0, pc_win = 0, pc_conv = 0, pc_ldw = 0;
+    long long pc_adv = 0, pc_bar = 0, pc_p1 = 0, pc_p2 = 0, pc_fin = 0;
+    uint32_t wgen = 0;
+    const long long p_start = T.prof ? clock64() : 0;
+    auto end_marker = [&]() {  // next tile slot: tells the MMA warp and the epilogue to stop
+      const uint32_t st = tile % NS;
+      if (tid == 0) {
+        wait_or_abort(&S.sfree[st], ((tile / NS) & 1) ^ 1, abort_flag, T.wait_limit);
+        S.meta[st].flags = FLAG_END;
+      }
+      prod_sync();
+      if (grp == 0) mbar_arrive(&S.full[st]);
+    };
+    for (;;) {
+      const long long cu0 = T.prof ? clock64() : 0;
+      const uint32_t slot = pf++ & 1;
+      if (tid == 0) {
+        const unsigned long long t = atomicAdd(&T.ctr->next_unit, 1ull);
+        const unsigned long long uu = t < T.n_def_in ? (unsigned long long)T.def_in[t] : T.main_start + (t - T.n_def_in);
+        S.unit = uu;
+        bool go = (T.claim_cap == 0 || t < T.claim_cap) && uu < T.n_units && !*abort_flag;
+        if (go && P.ring && *(volatile unsigned long long*)&P.ctr->stop) {
+          const RingCtx rc{P.pair_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
+          ring_defer(&rc, P.tag_base_tc + (uint32_t)uu);
+          go = false;
+        }
+        if (go && unit_k > 0) go = wait_or_abort(&S.afree, (unit_k - 1) & 1, abort_flag, T.wait_limit);
+        S.pflag[slot] = go ? 1u : 0u;
+      }
+      prod_sync();
+      if (!S.pflag[slot]) {
+        end_marker();
+        break;
+      }
+      const unsigned long long u = S.unit;
+      const Unit U = T.units[u];
+      const float* X = (const float*)P.xs;
+      const uint32_t *bstart = P.bstart, *nbr = P.nbr, *ids = P.ids;
+      TcBound tb = T.b;
+      uint32_t inst = 0;
+      if (T.unit_inst) {
+        inst = T.unit_inst[u];
+        const InstDesc& I = P.insts[inst];
+        X = (const float*)I.xs;
+        bstart = I.bstart;
+        nbr = I.nbr;
+        ids = I.ids;
+        tb = I.tcb;
+      }
+      if (P.ring) inst = P.tag_base_tc + (uint32_t)u;
+      const uint32_t hs = bstart[U.h], he = bstart[U.h + 1];
+      const uint32_t a0 = hs + U.chunk * (TM * G);
+      const uint32_t na = min((uint32_t)(TM * G), he - a0);
+      const uint32_t ng = (na + TM - 1) / TM;
+      if (tid < (int)P.dpad) {
+        const float c = X[(size_t)a0 * P.dpad + tid];
+        S.cadd_a[tid] = -c;
+        S.cadd_b[tid] = 2.f * c;
+      }
+      if (tid == 0) S.ra2max = 0;
+      prod_sync();
+      uint32_t my_aid[G];  // original ids of home rows g * TM + pr
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const uint32_t r = g * TM + pr;
+        my_aid[g] = r < na ? ids[a0 + r] : 0u;
+      }
+      {  // home rows r = tid + 256 i, whole rows
+        constexpr int HR = (G * TM + NPROD - 1) / NPROD;
+#pragma unroll
+        for (int i = 0; i < HR; ++i) {
+          const uint32_t r = (uint32_t)tid + NPROD * i;
+          if (r < na)
+            load_row<KP>(Ahi + (r / TM) * OPB, Alo + (r / TM) * OPB, r % TM, X + (size_t)(a0 + r) * P.dpad, P.dpad);
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        float m = 0.f;
+#pragma unroll
+        for (int i = 0; i < HR; ++i) {
+          const uint32_t r = (uint32_t)tid + NPROD * i;
+          if (r < na) {
+            __nv_bfloat16 *ah = Ahi + (r / TM) * OPB, *al = Alo + (r / TM) * OPB;
+            const float nrm = conv_row<KP>(ah, al, ah, al, r % TM, S.cadd_a, 1.f, P.d, 0.f, 1.f);
+            patch_col<KP>(ah, al, r % TM, P.d, nrm);
+            m = fmaxf(m, nrm);
+          }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL_MASK, m, o));
+        if (lane == 0) atomicMax(&S.ra2max, __float_as_uint(m));
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(&S.afull);
+      prod_sync();
+      const float ra2max = __uint_as_float(S.ra2max);
+      if (T.prof) pc_unit += clock64() - cu0;
+
+      // ---- candidate pairs of tiles of this unit
+      uint32_t seg_next = U.s0, w_nb = 0, w_pos = 0, w_total = 0;
+      unsigned long long pq = 0;  // per pair in flight: colsA | lastA << 8 | colsB << 9 | lastB << 17
+      uint32_t pin = 0;           // pairs in flight
+      int w_hj = -1;
+      auto home_cols = [&](uint32_t pos, uint32_t ncols, uint32_t* hcr, uint32_t* hq) {
+        *hcr = 0;
+        *hq = 0;
+        if (w_hj >= 0 && ncols > 0) {
+          const uint32_t hr0 = S.w_pref[w_hj], hr1 = S.w_pref[w_hj + 1];
+          if (max(hr0, pos) < min(hr1, pos + ncols)) {
+            const uint32_t lo = max(hr0, pos) - pos, hi = min(hr1, pos + ncols) - pos;
+            *hcr = lo | (hi << 8);
+            *hq = hs + (pos + lo - hr0);
+          }
+        }
+      };
+      // issues the next pair: returns 1, or 2 on abort
+      auto advance = [&]() -> int {
+        while (w_pos >= w_total) {
+          const long long cw0 = T.prof ? clock64() : 0;
+          const uint32_t nb = min((uint32_t)WIN, U.s1 - seg_next);
+          uint32_t st0 = 0, sz0 = 0, bn = 0xffffffffu;
+          if ((uint32_t)tid < nb) {
+            bn = nbr[seg_next + tid];
+            st0 = bstart[bn];
+            sz0 = bstart[bn + 1] - st0;
+          }
+          const uint32_t incl = warp_scan_incl(sz0);
+          if (lane == 31) S.scan_ws[warp] = incl;
+          prod_sync();
+          uint32_t wp = 0;
+          for (int w = 0; w < warp; ++w) wp += S.scan_ws[w];
+          ++wgen;
+          if ((uint32_t)tid < nb) {
+            S.w_start[tid] = st0;
+            S.w_pref[tid + 1] = wp + incl;
+            if (bn == U.h) S.w_home = ((wgen & 0xffffffu) << 8) | (uint32_t)tid;
+          }
+          if (tid == 0) S.w_pref[0] = 0;
+          prod_sync();
+          {
+            const uint32_t wh = S.w_home;
+            w_hj = (wh >> 8) == (wgen & 0xffffffu) ? (int)(wh & 255u) : -1;
+          }
+          w_nb = nb;
+          w_pos = 0;
+          w_total = S.w_pref[nb];
+          seg_next += nb;
+          if (T.prof) pc_win += clock64() - cw0;
+        }
+        const long long ca0 = T.prof ? clock64() : 0;
+        const uint32_t left = w_total - w_pos;
+        const uint32_t colsA = min((uint32_t)TN, left);
+        const uint32_t colsB = left > (uint32_t)TN ? min((uint32_t)TN, left - TN) : 0u;
+        const bool more = seg_next < U.s1;  // further windows after this one
+        const bool lastA = colsB == 0 && left <= (uint32_t)TN && !more;
+        const bool lastB = colsB > 0 && left <= 2u * TN && !more;
+        const uint32_t mycols = grp ? colsB : colsA;
+        // row of candidate rank w_pos + tid (warp-wide probes of the window prefix)
+        uint32_t q = 0xffffffffu;
+        {
+          const uint32_t r0 = w_pos + ((uint32_t)tid & ~31u);
+          const uint32_t step = (w_nb + 31) >> 5;
+          const uint32_t c = __popc(__ballot_sync(FULL_MASK, lane * step < w_nb && S.w_pref[lane * step] <= r0));
+          const uint32_t base = (c - 1) * step;
+          const uint32_t b0 =
+              base + __popc(__ballot_sync(FULL_MASK, (uint32_t)lane < step && base + lane < w_nb &&
+                                                         S.w_pref[base + lane] <= r0)) - 1;
+          const uint32_t e = b0 + 1 + lane;
+          const uint32_t t = e <= w_nb ? S.w_pref[e] - r0 : 32u;
+          const uint32_t bounds = __reduce_or_sync(FULL_MASK, t < 32u ? 1u << t : 0u);
+          if (pr < mycols) {
+            const uint32_t b = b0 + __popc(bounds & ((2u << lane) - 1u));
+            q = S.w_start[b] + (r0 + lane - S.w_pref[b]);
+          }
+        }
+        const uint32_t rs = (issued + grp) % RAW;
+        __nv_bfloat16* dh = Raw + rs * 2 * OPB;
+        __nv_bfloat16* dl = dh + OPB;
+        if (pr < mycols) {
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(&S.rid[rs][pr])), "l"(ids + q)
+                       : "memory");
+          load_row<KP>(dh, dl, pr, X + (size_t)q * P.dpad, P.dpad);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        if (tid == 0) {
+          uint32_t hcr, hq;
+          home_cols(w_pos, colsA, &hcr, &hq);
+          S.hx[issued & 3][0] = hcr;
+          S.hx[issued & 3][1] = hq;
+          home_cols(w_pos + TN, colsB, &hcr, &hq);
+          S.hx[(issued + 1) & 3][0] = hcr;
+          S.hx[(issued + 1) & 3][1] = hq;
+        }
+        pq |= (unsigned long long)(colsA | (lastA ? 0x100u : 0u) | (colsB << 9) | (lastB ? 0x20000u : 0u))
+              << (18 * pin);
+        ++pin;
+        w_pos += colsB > 0 ? 2u * TN : (uint32_t)TN;
+        issued += colsB > 0 ? 2u : 1u;
+        if (T.prof) pc_adv += clock64() - ca0;
+        return 1;
+      };
+
+      bool first = true, aborted = false;
+      for (;;) {
+        while (pin < 2 && (w_pos < w_total || seg_next < U.s1)) advance();
+        if (pin == 0) break;
+        const long long cc0 = T.prof ? clock64() : 0;
+        if (pin == 2)
+          asm volatile("cp.async.wait_group 1;" ::: "memory");
+        else
+          asm volatile("cp.async.wait_group 0;" ::: "memory");
+        if (T.prof) pc_ldw += clock64() - cc0;
+        const uint32_t e = (uint32_t)(pq & 0x3ffffull);
+        pq >>= 18;
+        --pin;
+        const uint32_t colsA = e & 0xffu, colsB = (e >> 9) & 0xffu;
+        const bool lastA = (e & 0x100u) != 0u, lastB = (e & 0x20000u) != 0u;
+        const uint32_t nt = colsB > 0 ? 2u : 1u;
+        const long long cb0 = T.prof ? clock64() : 0;
+        const uint32_t fl = pf++ & 1;
+        if (tid == 0) {
+          const long long c0 = T.prof ? clock64() : 0;
+          bool ok = wait_or_abort(&S.sfree[tile % NS], ((tile / NS) & 1) ^ 1, abort_flag, T.wait_limit);
+          if (ok && nt == 2)
+            ok = wait_or_abort(&S.sfree[(tile + 1) % NS], (((tile + 1) / NS) & 1) ^ 1, abort_flag, T.wait_limit);
+          S.pflag[fl] = ok ? 1u : 0u;
+          if (T.prof) pw_sfree += clock64() - c0;
+        }
+        prod_sync();
+        if (T.prof) pc_bar += clock64() - cb0;
+        if (!S.pflag[fl]) {
+          aborted = true;
+          break;
+        }
+        if (grp < nt) {
+          const uint32_t mt = tile + grp;
+          const uint32_t st = mt % NS, rs = mt % RAW;
+          const uint32_t ncols = grp ? colsB : colsA;
+          const bool last = grp ? lastB : lastA;
+          const bool ok = pr < ncols;
+          __nv_bfloat16* bh = Bhi + st * OPB;
+          __nv_bfloat16* bl = Blo + st * OPB;
+          const long long cp0 = T.prof ? clock64() : 0;
+          if (ok) {
+            const __nv_bfloat16* sh = Raw + rs * 2 * OPB;
+            S.qid[st][pr] = S.rid[rs][pr];
+            const float nq2 = conv_row<KP>(sh, sh + OPB, bh, bl, pr, S.cadd_b, -2.f, P.d, 1.f, 0.f) * 0.25f;
+            float tcol = 0.f, dl = 0.f;
+            if (!column_threshold(tb, ra2max, nq2, &tcol, &dl)) {
+              tcol = 1e30f;   // every row of this column becomes a candidate ...
+              dl = INFINITY;  // ... and none is accepted without the FP64 check
+            }
+            patch_col<KP>(bh, bl, pr, P.d + 1, nq2 - tcol);
+            S.dlt[st][pr] = dl;
+          }
+          const long long cp1 = T.prof ? clock64() : 0;
+#pragma unroll
+          for (int g = 0; g < G; ++g) S.aid[st][g * TM + pr] = my_aid[g];
+          if (pr == 0) {
+            S.meta[st] = TileMeta{a0, na, ncols, (first && grp == 0 ? FLAG_FIRST : 0u) | (last ? FLAG_LAST : 0u), ng,
+                                  S.hx[mt & 3][0], S.hx[mt & 3][1], inst};
+            n_tiles += 1;
+            n_cells += (unsigned long long)na * ncols;
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          mbar_arrive(&S.full[st]);
+          if (T.prof) {
+            const long long ce = clock64();
+            pc_p1 += cp1 - cp0;
+            pc_fin += ce - cp1;
+            pc_conv += ce - cc0;
+          }
+        }
+        first = false;
+        tile += nt;
+      }
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      ++unit_k;
+      if (aborted) {
+        end_marker();
+        break;
+      }
+    }
+    if (pr == 0 && n_tiles) {
+      atomicAdd(&T.ctr->tiles, n_tiles);
+      atomicAdd(&T.ctr->cells, n_cells);
+    }
+    if (tid == 0 && T.prof) {
+      atomicAdd(&T.ctr->prof[0], (unsigned long long)pw_sfree);
+      atomicAdd(&T.ctr->prof[1], (unsigned long long)(clock64() - p_start));
+      atomicAdd(&T.ctr->prof[7], (unsigned long long)pc_unit);
+      atomicAdd(&T.ctr->prof[8], (unsigned long long)pc_win);
+      atomicAdd(&T.ctr->prof[9], (unsigned long long)pc_conv);
+      atomicAdd(&T.ctr->prof[14], (unsigned long long)pc_ldw);
+      atomicAdd(&T.ctr->prof[16], (unsigned long long)pc_adv);
+      atomicAdd(&T.ctr->prof[17], (unsigned long long)pc_bar);
+      atomicAdd(&T.ctr->prof[18], (unsigned long long)pc_p1);
+      atomicAdd(&T.ctr->prof[19], (unsigned long long)pc_p2);
+      atomicAdd(&T.ctr->prof[20], (unsigned long long)pc_fin);
+    }
+    } else {
     // ============================ producers (NPW warps, two threads per row)
     // Thread (prow, half): row prow = 32 * (warp % 4) + lane of every operand
     // tile, K blocks kb = 2j + half with half = warp / 4, so the lanes of a
@@ -610,6 +981,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
       atomicAdd(&T.ctr->prof[19], (unsigned long long)pc_p2);
       atomicAdd(&T.ctr->prof[20], (unsigned long long)pc_fin);
     }
+    }  // two threads a row
   } else if (warp == MMA_WARP) {
     // ============================ MMA issuer
     // B tiles come in stage order; each is multiplied with the unit's ng home
@@ -830,7 +1202,9 @@ template <int KP>
 struct TcShape {
   static constexpr int G = KP <= 32 ? 4 : (KP <= 64 ? 2 : 1);
   static constexpr int NS = KP <= 32 ? 4 : (KP <= 96 ? 3 : 2);
-  static constexpr int RAW = KP <= 48 ? 3 : 0;  // separate landing slots where they fit
+  // separate landing slots where they fit: four for K <= 32 (pair mode, two
+  // pairs of tiles in flight), three for K = 48
+  static constexpr int RAW = KP <= 32 ? 4 : (KP <= 48 ? 3 : 0);
   // short rows: many tiles, pairs and hits per converted row -> more epilogue
   // warps (16: 72 registers a thread); long rows: 8 (96 registers)
   static constexpr int NEPI = KP <= 48 ? 16 : 8;
