@@ -26,6 +26,8 @@
 #include <cstdio>
 #include <cstdlib>
 
+#include <type_traits>
+
 #include "emit.cuh"
 #include "internal.cuh"
 
@@ -398,21 +400,22 @@ k_join_f32r(const JoinParams P) {
 #pragma unroll
       for (int c = 0; c < DQ; ++c) qq[c] = qrow[c];
       uint32_t m = 0, lo_m = 0;
+      // home rows in groups of 8 independent chains; a last group of at most
+      // 4 rows (small bins: most home chunks hold a few points) takes 4.
+      // Packed FP32 pairs (Blackwell f32x2, per-lane IEEE rounding): each
+      // home row accumulates its even and odd coordinates separately and
+      // adds the two sums at the end; the filter's error bound holds for any
+      // summation order, and half the instructions are issued
+      auto rows = [&](auto nr_tag, int r0) {
+        constexpr int NR = decltype(nr_tag)::value;
+        unsigned long long acc2[NR];
 #pragma unroll
-      for (int g = 0; g < CH / 8; ++g) {
-        if (g * 8 >= (int)na) break;
-        // packed FP32 pairs (Blackwell f32x2, per-lane IEEE rounding): each
-        // home row accumulates its even and odd coordinates separately and
-        // adds the two sums at the end; the filter's error bound holds for
-        // any summation order, and half the instructions are issued
-        unsigned long long acc2[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) acc2[i] = 0ull;
+        for (int i = 0; i < NR; ++i) acc2[i] = 0ull;
 #pragma unroll
         for (int c = 0; c < DQ; ++c) {
 #pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const ulonglong2 aa = reinterpret_cast<const ulonglong2*>(sA)[(g * 8 + i) * DQ + c];
+          for (int i = 0; i < NR; ++i) {
+            const ulonglong2 aa = reinterpret_cast<const ulonglong2*>(sA)[(r0 + i) * DQ + c];
             unsigned long long tt;
             asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(tt) : "l"(aa.x), "l"(qq[c].x));
             asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[i]) : "l"(tt));
@@ -421,13 +424,21 @@ k_join_f32r(const JoinParams P) {
           }
         }
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < NR; ++i) {
           float lo, hi;
           asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(acc2[i]));
           const float acc = lo + hi;
-          m |= (acc <= V.t_hi ? 1u : 0u) << (g * 8 + i);
-          lo_m |= (acc <= V.t_lo ? 1u : 0u) << (g * 8 + i);
+          m |= (acc <= V.t_hi ? 1u : 0u) << (r0 + i);
+          lo_m |= (acc <= V.t_lo ? 1u : 0u) << (r0 + i);
         }
+      };
+#pragma unroll
+      for (int g = 0; g < CH / 8; ++g) {
+        if (g * 8 >= (int)na) break;
+        if ((int)na - g * 8 <= 4)
+          rows(std::integral_constant<int, 4>{}, g * 8);
+        else
+          rows(std::integral_constant<int, 8>{}, g * 8);
       }
       m = t.qv ? (m & home_mask(na, q >= hs && q < he, q, a0, CH)) : 0u;
       if (__any_sync(FULL_MASK, m != 0)) {

@@ -72,7 +72,7 @@ constexpr int WNS = 3;       // stages
 constexpr int WWIN = 256;    // neighbour bins per candidate window
 constexpr int WNPW = 8;      // producer warps: thread t loads home row t and candidate row t
 constexpr int WNPROD = WNPW * 32;
-constexpr int WNEPI = 8;     // epilogue warps: 4 TMEM lane quarters x 2 column halves
+constexpr int WNEPI = 16;    // epilogue warps: 4 TMEM lane quarters x 4 column groups
 constexpr int WEPI0 = WNPW;  // first epilogue warp (a multiple of 4: warp % 4 is its lane quarter)
 constexpr int WMMA = WEPI0 + WNEPI;
 constexpr int WTHREADS = (WMMA + 1) * 32;
@@ -257,7 +257,7 @@ __global__ void k_tf32_rows(const float* __restrict__ xf, uint32_t dpad32, uint3
 }
 
 // ---------------------------------------------------------------- pipeline
-// One persistent CTA per SM: 8 producer warps, 8 epilogue warps, 1 MMA warp.
+// One persistent CTA per SM: 8 producer warps, 16 epilogue warps, 1 MMA warp.
 //   producers  fetch units; per group of up to 256 candidates all 8 warps
 //              compute the columns' sorted positions, ids, norms and
 //              thresholds; warp 0 then issues, per K chunk, the stage's TMA
