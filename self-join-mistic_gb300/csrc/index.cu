@@ -367,8 +367,93 @@ __device__ __forceinline__ bool group_sampled(uint32_t h, uint32_t g, uint32_t S
   return x % S == 0;
 }
 
+// Field j of key K: bits [shift[j], shift[j-1]) (shift[-1] = 64).
+__device__ __forceinline__ int key_field(uint64_t K, const EnumParams& P, int j) {
+  const int hi_bit = j == 0 ? 64 : P.shift[j - 1];
+  const int width = hi_bit - P.shift[j];
+  const uint64_t mask = width >= 64 ? ~0ull : ((1ull << width) - 1ull);
+  return (int)((K >> P.shift[j]) & mask);
+}
+
+// The same walk for any depth, with its per-level state in arrays (local
+// memory): used below the levels walk_levels keeps in registers.
+template <class Leaf>
+__device__ __noinline__ void walk_deep(const uint64_t* __restrict__ bkey, uint64_t K, uint32_t hb,
+                                       const EnumParams& P, int j0, uint32_t lo0, uint32_t hi0, uint64_t base0,
+                                       Leaf& leaf) {
+  uint32_t lo[MAX_K + 1], hi[MAX_K + 1];
+  uint64_t base[MAX_K + 1];
+  int di[MAX_K + 1];
+  lo[j0] = lo0;
+  hi[j0] = hi0;
+  base[j0] = base0;
+  di[j0] = 0;
+  int j = j0;
+  while (j >= j0) {
+    if (di[j] == 3) {
+      --j;
+      if (j >= j0) ++di[j];
+      continue;
+    }
+    const int cv = key_field(K, P, j) + di[j] - 1;
+    if (cv < 0 || (long long)cv > (long long)P.maxkey[j]) {
+      ++di[j];
+      continue;
+    }
+    const uint64_t lower = base[j] | ((uint64_t)cv << P.shift[j]);
+    const uint64_t upper = lower + (1ull << P.shift[j]);
+    const uint32_t a = lower_bound_u64(bkey, lo[j], hi[j], lower);
+    const uint32_t b = lower_bound_u64(bkey, a, hi[j], upper);
+    if (a == b || b <= hb) {
+      ++di[j];
+      continue;
+    }
+    if (j == P.k - 1) {
+      leaf(a);
+      ++di[j];
+      continue;
+    }
+    base[j + 1] = lower;
+    lo[j + 1] = a;
+    hi[j + 1] = b;
+    di[j + 1] = 0;
+    ++j;
+  }
+}
+
+// Depth-first walk of key fields j .. k-1 of home key K inside the sorted bin
+// range [lo, hi) whose keys share the prefix bits `base`: field values
+// K_j - 1, K_j, K_j + 1 in order, each narrowed by two lower-bound searches;
+// leaf(a) for every bin a >= hb, in ascending order.  The first R levels
+// keep their range and loop state in registers; deeper ones go to walk_deep.
+template <int R, class Leaf>
+__device__ __forceinline__ void walk_levels(const uint64_t* __restrict__ bkey, uint64_t K, uint32_t hb,
+                                            const EnumParams& P, int j, uint32_t lo, uint32_t hi, uint64_t base,
+                                            Leaf& leaf) {
+  const int sh = P.shift[j];
+  const int kfj = key_field(K, P, j);
+#pragma unroll 1
+  for (int di = 0; di < 3; ++di) {
+    const int cv = kfj + di - 1;
+    if (cv < 0 || (long long)cv > (long long)P.maxkey[j]) continue;
+    const uint64_t lower = base | ((uint64_t)cv << sh);
+    const uint64_t upper = lower + (1ull << sh);
+    const uint32_t a = lower_bound_u64(bkey, lo, hi, lower);
+    const uint32_t b = lower_bound_u64(bkey, a, hi, upper);
+    if (a == b || b <= hb) continue;
+    if (j == P.k - 1) {
+      leaf(a);  // b == a + 1 and a >= hb
+      continue;
+    }
+    if constexpr (R > 1)
+      walk_levels<R - 1>(bkey, K, hb, P, j + 1, a, b, lower, leaf);
+    else
+      walk_deep(bkey, K, hb, P, j + 1, a, b, lower, leaf);
+  }
+}
+
 template <bool FILL>
-__global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __restrict__ bstart,
+__global__ void __launch_bounds__(128, 8) k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __restrict__ bstart,
                        uint32_t m, EnumParams P, uint32_t* __restrict__ nbr_cnt,
                        uint32_t* __restrict__ unit_cnt, uint32_t* __restrict__ unit_cnt_tc,
                        unsigned long long* __restrict__ cand, const uint32_t* __restrict__ nbr_off,
@@ -399,23 +484,6 @@ __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __rest
     }
   }
 
-  int kf[MAX_K];
-  // decode fields: field j spans [shift[j], shift[j-1]) (shift[-1] = 64)
-  for (int j = 0; j < P.k; ++j) {
-    const int hi_bit = j == 0 ? 64 : P.shift[j - 1];
-    const int width = hi_bit - P.shift[j];
-    const uint64_t mask = width >= 64 ? ~0ull : ((1ull << width) - 1ull);
-    kf[j] = (int)((K >> P.shift[j]) & mask);
-  }
-
-  uint32_t lo[MAX_K + 1], hi[MAX_K + 1];
-  uint64_t base[MAX_K + 1];
-  int di[MAX_K + 1];
-  lo[0] = 0;
-  hi[0] = m;
-  base[0] = 0;
-  di[0] = 0;
-  int j = 0;
 
   uint32_t cnt = 0, nseg = 0, seg_fill = 0, seg_begin = 0;
   unsigned long long c = 0;
@@ -442,58 +510,24 @@ __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __rest
     ++cnt;
   };
 
-  // the walk below level j0 of the range [lo[j0], hi[j0]) with prefix base[j0]
-  auto walk = [&](int j0) {
-  j = j0;
-  while (j >= j0) {
-    if (di[j] == 3) {
-      --j;
-      if (j >= j0) ++di[j];
-      continue;
-    }
-    const int cv = kf[j] + di[j] - 1;
-    if (cv < 0 || (long long)cv > (long long)P.maxkey[j]) {
-      ++di[j];
-      continue;
-    }
-    const uint64_t lower = base[j] | ((uint64_t)cv << P.shift[j]);
-    const uint64_t upper = lower + (1ull << P.shift[j]);
-    const uint32_t a = lower_bound_u64(bkey, lo[j], hi[j], lower);
-    const uint32_t b = lower_bound_u64(bkey, a, hi[j], upper);
-    if (a == b || b <= hb) {
-      ++di[j];
-      continue;
-    }
-    if (j == P.k - 1) {
-      leaf(a);  // b == a + 1 and a >= hb
-      ++di[j];
-      continue;
-    }
-    base[j + 1] = lower;
-    lo[j + 1] = a;
-    hi[j + 1] = b;
-    di[j + 1] = 0;
-    ++j;
-  }
-  };
   if (P.k == 0) {
     leaf(hb);  // no key fields: one bin holding every point
   } else if (P.p == 0) {
-    walk(0);
+    walk_levels<3>(bkey, K, hb, P, 0, 0u, m, 0ull, leaf);
   } else {
     // prefixes in ascending order: field j offset by digit j of c in base 3
     // (field 0 most significant)
     uint32_t n3 = 1;
     for (int q = 0; q < P.p; ++q) n3 *= 3;
-    for (uint32_t c = 0; c < n3; ++c) {
-      uint32_t rem = c, pw = n3 / 3, idx = 0;
+    for (uint32_t cb = 0; cb < n3; ++cb) {
+      uint32_t rem = cb, pw = n3 / 3, idx = 0;
       uint64_t pre = 0;
       bool ok = true;
       for (int q = 0; q < P.p; ++q) {
         const uint32_t t = rem / pw;
         rem -= t * pw;
         pw /= 3;
-        const int cv = kf[q] + (int)t - 1;
+        const int cv = key_field(K, P, q) + (int)t - 1;
         if (cv < 0 || (uint32_t)cv > P.maxkey[q]) {
           ok = false;
           break;
@@ -508,11 +542,7 @@ __global__ void k_enum(const uint64_t* __restrict__ bkey, const uint32_t* __rest
         leaf(r0);
         continue;
       }
-      lo[P.p] = r0;
-      hi[P.p] = r1;
-      base[P.p] = pre;
-      di[P.p] = 0;
-      walk(P.p);
+      walk_levels<3>(bkey, K, hb, P, P.p, r0, r1, pre, leaf);
     }
   }
   if (cnt > 0) {

@@ -628,6 +628,59 @@ __global__ void __launch_bounds__(WTHREADS, 1)
         const uint32_t ng = Gm.ng;
         const uint32_t nmma = max(16u, (Gm.ncols + 15u) & ~15u);  // MMA N: the group's columns, rounded to 16
         const uint32_t idesc = umma_idesc_fmt(WM, (int)nmma, PREC == 2 ? 2u : 1u);
+        // MMAs of home chunk g for K chunk kc from stage s
+        auto issue = [&](uint32_t g, uint32_t kc, uint32_t s) {
+          const uint32_t sb = stage_base + s * STAGE_BYTES;
+          const uint32_t bh = sb + B_HI, bl = sb + B_LO;
+          const uint32_t dt = tbase + g * WN;
+          if (PREC == 0) {
+            const uint32_t ah = sb + g * A_CHUNK, al = sb + A_LO + g * A_CHUNK;
+#pragma unroll
+            for (int ks = 0; ks < WKC / 16; ++ks) {
+              // K step of 16 bf16: 32 bytes into the 64-byte swizzled rows of
+              // both operands
+              const uint32_t ok16 = ks * 32;
+              const uint64_t dah = desc_sw64(ah + ok16), dal = desc_sw64(al + ok16);
+              const uint64_t dbh = desc_sw64(bh + ok16), dbl = desc_sw64(bl + ok16);
+              mma_bf16(dt, dah, dbh, idesc, (kc | ks) ? 1u : 0u);
+              mma_bf16(dt, dah, dbl, idesc, 1u);
+              mma_bf16(dt, dal, dbh, idesc, 1u);
+            }
+          } else {
+            const uint32_t a1 = sb + g * S_ACHUNK, b1 = sb + S_B;
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              // one K step (16 bf16 or 8 tf32) = 32 bytes into the 128-byte
+              // swizzled rows of both operands
+              const uint64_t da = desc_sw128(a1 + ks * 32), db = desc_sw128(b1 + ks * 32);
+              if (PREC == 2)
+                mma_tf32(dt, da, db, idesc, (kc | ks) ? 1u : 0u);
+              else
+                mma_bf16(dt, da, db, idesc, (kc | ks) ? 1u : 0u);
+            }
+          }
+        };
+        auto release = [&](uint32_t st) {  // the stage of global step st may be refilled once its MMAs have read it
+          tc_commit(&S.sfree[st % WNS]);
+          last_bar = &S.sfree[st % WNS];
+          last_par = (st / WNS) & 1;
+        };
+        // Accumulator 1 may still be drained by the epilogue when the group
+        // starts; rather than wait, chunk 0 runs ahead through the stages
+        // already full, and chunk 1 catches up on them (their release is
+        // held back) once accumulator 1 is free.  nd stages are deferred,
+        // from global step d0; all stages deferred means the ring is full,
+        // and then the lane waits.
+        const uint32_t step0 = step;
+        uint32_t nd = 0, d0 = 0;
+        auto catch_up = [&]() {
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          for (uint32_t i = 0; i < nd; ++i) {
+            issue(1, d0 + i - step0, (d0 + i) % WNS);
+            release(d0 + i);
+          }
+          nd = 0;
+        };
         for (uint32_t kc = 0; kc < nkc && ok; ++kc) {
           if (kc > 0) {
             s = step % WNS;
@@ -642,48 +695,36 @@ __global__ void __launch_bounds__(WTHREADS, 1)
           // are read by the MMAs (async proxy): this thread has acquired them
           // through the full barrier; order them before its MMAs
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          const uint32_t sb = stage_base + s * STAGE_BYTES;
-          const uint32_t bh = sb + B_HI, bl = sb + B_LO;
-          for (uint32_t g = 0; g < ng; ++g) {
-            if (kc == 0) {  // first writes of this group into accumulator g
+          if (kc == 0) {  // first writes of this group into accumulator 0
+            const long long c2 = T.prof ? clock64() : 0;
+            ok = wait_or_abort(&S.dfree[0], (use[0] & 1) ^ 1, abort_flag, T.wait_limit);
+            if (T.prof) mw_dfree += clock64() - c2;
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+          }
+          issue(0, kc, s);
+          if (ng > 1) {
+            if (nd > 0 && mbar_ready(&S.dfree[1], (use[1] & 1) ^ 1)) catch_up();
+            if (nd > 0) {
+              ++nd;  // this stage's chunk 1 waits too
+            } else if (kc == 0 && !mbar_ready(&S.dfree[1], (use[1] & 1) ^ 1)) {
+              nd = 1;
+              d0 = step;
+            } else {
+              if (kc == 0) asm volatile("tcgen05.fence::after_thread_sync;");
+              issue(1, kc, s);
+              release(step);
+            }
+            if (nd >= (uint32_t)WNS || (nd > 0 && kc + 1 == nkc)) {  // ring held or group done: wait for accumulator 1
               const long long c2 = T.prof ? clock64() : 0;
-              ok = wait_or_abort(&S.dfree[g], (use[g] & 1) ^ 1, abort_flag, T.wait_limit);
+              ok = wait_or_abort(&S.dfree[1], (use[1] & 1) ^ 1, abort_flag, T.wait_limit);
               if (T.prof) mw_dfree += clock64() - c2;
               if (!ok) break;
-              asm volatile("tcgen05.fence::after_thread_sync;");
+              catch_up();
             }
-            const uint32_t dt = tbase + g * WN;
-            if (PREC == 0) {
-              const uint32_t ah = sb + g * A_CHUNK, al = sb + A_LO + g * A_CHUNK;
-#pragma unroll
-              for (int ks = 0; ks < WKC / 16; ++ks) {
-                // K step of 16 bf16: 32 bytes into the 64-byte swizzled rows of
-                // both operands
-                const uint32_t ok16 = ks * 32;
-                const uint64_t dah = desc_sw64(ah + ok16), dal = desc_sw64(al + ok16);
-                const uint64_t dbh = desc_sw64(bh + ok16), dbl = desc_sw64(bl + ok16);
-                mma_bf16(dt, dah, dbh, idesc, (kc | ks) ? 1u : 0u);
-                mma_bf16(dt, dah, dbl, idesc, 1u);
-                mma_bf16(dt, dal, dbh, idesc, 1u);
-              }
-            } else {
-              const uint32_t a1 = sb + g * S_ACHUNK, b1 = sb + S_B;
-#pragma unroll
-              for (int ks = 0; ks < 4; ++ks) {
-                // one K step (16 bf16 or 8 tf32) = 32 bytes into the 128-byte
-                // swizzled rows of both operands
-                const uint64_t da = desc_sw128(a1 + ks * 32), db = desc_sw128(b1 + ks * 32);
-                if (PREC == 2)
-                  mma_tf32(dt, da, db, idesc, (kc | ks) ? 1u : 0u);
-                else
-                  mma_bf16(dt, da, db, idesc, (kc | ks) ? 1u : 0u);
-              }
-            }
+          } else {
+            release(step);
           }
-          if (!ok) break;
-          tc_commit(&S.sfree[s]);  // the stage may be refilled once these MMAs have read it
-          last_bar = &S.sfree[s];
-          last_par = (step / WNS) & 1;
           ++step;
         }
         if (!ok) break;

@@ -92,6 +92,16 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
+// Non-blocking test of an mbarrier phase.
+__device__ __forceinline__ bool mbar_ready(unsigned long long* b, uint32_t parity) {
+  uint32_t done;
+  asm volatile("{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(done)
+               : "r"(smem_u32(b)), "r"(parity)
+               : "memory");
+  return done != 0;
+}
+
 // Bounded wait on an mbarrier phase.  The waiting warp is suspended by the
 // hardware (try_wait with a suspend-time hint) instead of spinning, so idle
 // roles leave the issue slots to the working ones.  After limit_ns of
