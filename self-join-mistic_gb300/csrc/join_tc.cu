@@ -1119,7 +1119,8 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         uint32_t acc_bits = 0, band_bits = 0;
         const bool maybe = m != 0;
         const long long cs0 = T.prof ? clock64() : 0;
-        if (__any_sync(FULL_MASK, maybe)) {
+        const bool any_maybe = __any_sync(FULL_MASK, maybe);  // blocks without candidates skip the rest
+        if (any_maybe) {
           if (maybe) {
             // home bin: a pair (a, q) of two home rows is kept only for a < q
             // (sorted positions); the home rows of this tile are the columns
@@ -1157,9 +1158,9 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
               },
               counter, list, lcap, ip, M.inst, rc);
         };
-        if (__any_sync(FULL_MASK, acc_bits != 0u))
+        if (any_maybe && __any_sync(FULL_MASK, acc_bits != 0u))
           emit(ps, acc_bits, &P.ctr->pairs, P.pairs, P.cap, P.inst_pairs, rcp);
-        if (__any_sync(FULL_MASK, band_bits != 0u))
+        if (any_maybe && __any_sync(FULL_MASK, band_bits != 0u))
           emit(bs, band_bits, &P.ctr->band_n, P.band_list, P.band_cap, nullptr, rcb);
         if (T.prof) ec_stage += clock64() - cs1;
       }

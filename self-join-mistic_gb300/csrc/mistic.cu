@@ -515,7 +515,7 @@ bool tune_lookup(mistic_handle_s* h, const mistic_opts& o, uint32_t d, mistic_dt
   }
   const int eps_cls = (eps2 > 0 && R > 0) ? (int)std::floor(std::log2(R * R / eps2)) : 0;
   char key[160];
-  snprintf(key, sizeof key, "v3 d=%u dt=%d %s bins=%d,%d r2e=%d", d, (int)dt, wide ? "tcw" : "tc", c50, c90, eps_cls);
+  snprintf(key, sizeof key, "v4 d=%u dt=%d %s bins=%d,%d r2e=%d", d, (int)dt, wide ? "tcw" : "tc", c50, c90, eps_cls);
   if (tune_cache().find(key, out)) return true;
   // candidates
   std::vector<TuneCandidate> cands;
@@ -525,7 +525,8 @@ bool tune_lookup(mistic_handle_s* h, const mistic_opts& o, uint32_t d, mistic_dt
     for (int pr : precs) cands.push_back({1u, pr});  // every bin on the tensor cores (see tc_min_bin)
   } else {
     const uint32_t t0 = tc_min_bin(d, false);
-    for (uint32_t t : {std::max(1u, t0 / 2), t0, std::min(512u, 2 * t0)})
+    for (uint32_t t : {std::max(1u, t0 / 2), std::max(1u, 3 * t0 / 4), t0, std::min(512u, 3 * t0 / 2),
+                       std::min(512u, 2 * t0)})
       if (cands.empty() || cands.back().tc_min != t) cands.push_back({t, 0});
   }
   // sample: about 1/64 of the home points, but enough work units that the

@@ -23,7 +23,7 @@ def test_tuner_writes_and_reuses_the_cache(handle, monkeypatch, tmp_path):
     assert r1.tuned and r1.tc_min_bin >= 1
     assert np.array_equal(r1.pairs, ref), diff_pairs(r1.pairs, ref)
     lines = cache.read_text().strip().splitlines()
-    assert len(lines) == 1 and lines[0].startswith("v3 d=18")
+    assert len(lines) == 1 and lines[0].startswith("v4 d=18")
     key, tc_min, prec, ms = lines[0].split("\t")
     assert int(tc_min) == r1.tc_min_bin and int(prec) == 0 and float(ms) > 0
     r2 = handle.selfjoin(x, 6, eps, pairs="host", sort_pairs=True, autotune=1)
