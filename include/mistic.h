@@ -87,7 +87,11 @@ typedef enum mistic_mode {
 typedef enum mistic_rp_mode {
   MISTIC_RP_PCA = 0,  /* k far points along the sample's top-k principal axes (default) */
   MISTIC_RP_BOX = 1,  /* k points uniform in the bounding box (seeded) */
-  MISTIC_RP_USER = 2  /* caller-supplied k x d FP64 points in opts.rp_user */
+  MISTIC_RP_USER = 2, /* caller-supplied k x d FP64 points in opts.rp_user */
+  MISTIC_RP_SCORED = 3 /* the reference's per-layer selection (src/nodes.cu:168-222): layer by layer,
+                          the candidate (far points along principal axes, sample points, box
+                          points) leaving the fewest sample pairs within one eps-wide field on
+                          every chosen layer */
 } mistic_rp_mode;
 
 typedef enum mistic_pairs_where {

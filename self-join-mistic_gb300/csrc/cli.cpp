@@ -13,7 +13,7 @@
 // Options (none exist in the reference):
 //   --f32              input file holds FP32 rows
 //   --mode auto|fp64|fp32|bf16|tf32
-//   --rp pca|box       reference-point placement
+//   --rp pca|box|scored  reference-point placement
 //   --seed S
 //   --pairs out.bin    write the i<j pair list as uint32 (i, j) rows, sorted
 //   --device N
@@ -33,7 +33,7 @@
 static int usage(const char* p) {
   fprintf(stderr,
           "usage: %s <file.bin> <dim> <numRP> <epsilon> [--f32] [--mode auto|fp64|fp32|bf16|tf32] "
-          "[--rp pca|box] [--seed S] [--pairs out.bin] [--device N]\n"
+          "[--rp pca|box|scored] [--seed S] [--pairs out.bin] [--device N]\n"
           "       %s --to-bin <in.txt> <out.bin>\n",
           p, p);
   return 2;
@@ -78,7 +78,7 @@ int main(int argc, char** argv) {
     } else if (a == "--rp") {
       const char* v = next();
       if (!v) return usage(argv[0]);
-      o.rp_mode = std::string(v) == "box" ? MISTIC_RP_BOX : MISTIC_RP_PCA;
+      o.rp_mode = std::string(v) == "box" ? MISTIC_RP_BOX : (std::string(v) == "scored" ? MISTIC_RP_SCORED : MISTIC_RP_PCA);
     } else if (a == "--seed") {
       const char* v = next();
       if (!v) return usage(argv[0]);

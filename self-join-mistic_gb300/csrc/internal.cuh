@@ -337,6 +337,12 @@ void bruteforce_rows(mistic_handle_s* h, const void* x, mistic_dtype dt, uint64_
 
 // ---- rp.cpp: reference-point selection on the host.
 // stats: per-dim mean (d), min (d), max (d); cov: d x d sample covariance.
+// The reference's per-layer candidate scoring on a host copy of the data
+// sample (S x d rows): k points chosen greedily (MISTIC_RP_SCORED).
+void select_reference_points_scored(const mistic_opts& o, uint32_t d, uint32_t k, double eps,
+                                    const std::vector<double>& mean, const std::vector<double>& mn,
+                                    const std::vector<double>& mx, const std::vector<double>& cov,
+                                    const std::vector<double>& sample, uint32_t S, std::vector<double>& rps);
 void select_reference_points(const mistic_opts& o, uint32_t d, uint32_t k,
                              const std::vector<double>& mean,
                              const std::vector<double>& mn,

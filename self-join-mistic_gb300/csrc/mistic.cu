@@ -702,11 +702,13 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   unsigned* flag = abuf<unsigned>(h, "flag", 4);
   MCK(cudaMemsetAsync(flag, 0, 4 * sizeof(unsigned), h->stream));
   idx::colstats(h, x, dt, n, d, cs_part, cs_parts, cs_out, flag);
-  const bool pca = (o.rp_mode == MISTIC_RP_PCA) && k > 0 && d >= 2 && d <= 1024;
+  const bool scored = o.rp_mode == MISTIC_RP_SCORED && k > 0 && d >= 2 && d <= 1024;
+  const bool pca = (o.rp_mode == MISTIC_RP_PCA || scored) && k > 0 && d >= 2 && d <= 1024;
   const uint32_t S = (uint32_t)std::min<uint64_t>(n, d <= 64 ? 8192 : 4096);
   double* cov = nullptr;
+  double* sbuf = nullptr;
   if (pca) {
-    double* sbuf = abuf<double>(h, "sample", (size_t)S * d);
+    sbuf = abuf<double>(h, "sample", (size_t)S * d);
     cov = abuf<double>(h, "cov", (size_t)d * d);
     double* cpart = abuf<double>(h, "cov_part", (size_t)((S + 127) / 128) * d * d);
     idx::sample_cov(h, x, dt, n, d, S, sbuf, cs_out /* full-data column means */, cpart, cov);
@@ -724,7 +726,13 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     d2h(h, covh.data(), cov, covh.size() * sizeof(double));
   }
   std::vector<double> rps;
-  select_reference_points(o, d, k, mean, mn, mx, covh, rps);
+  if (scored) {
+    std::vector<double> sh((size_t)S * d);
+    d2h(h, sh.data(), sbuf, sh.size() * sizeof(double));
+    select_reference_points_scored(o, d, k, eps, mean, mn, mx, covh, sh, S, rps);
+  } else {
+    select_reference_points(o, d, k, mean, mn, mx, covh, rps);
+  }
   clk.mark();  // 2
 
   // ---- FP64 reference-point distances, key layout, packed keys

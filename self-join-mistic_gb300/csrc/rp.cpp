@@ -136,4 +136,85 @@ void select_reference_points(const mistic_opts& o, uint32_t d, uint32_t k, const
   }
 }
 
+// Scored reference points (MISTIC_RP_SCORED): the reference's per-layer
+// selection, buildNodeNet's candidate scoring (src/nodes.cu:168-222) over
+// createRPArray's candidate sets (src/utils.cu:66-136), restated: layer by
+// layer, every candidate point bins a sample of the data into eps-wide
+// distance fields, and the candidate that leaves the fewest sample pairs
+// within one field of each other on every layer chosen so far (the
+// neighbour relation of the join) is kept.  Candidates: far points along the
+// sample's leading principal axes on both sides, sample points, and seeded
+// box points.
+void select_reference_points_scored(const mistic_opts& o, uint32_t d, uint32_t k, double eps,
+                                    const std::vector<double>& mean, const std::vector<double>& mn,
+                                    const std::vector<double>& mx, const std::vector<double>& cov,
+                                    const std::vector<double>& sample, uint32_t S, std::vector<double>& rps) {
+  rps.assign((size_t)k * d, 0.0);
+  if (k == 0) return;
+  // candidate pool
+  const uint32_t na = std::min<uint32_t>(2 * k, d);
+  std::vector<double> pca;
+  {
+    mistic_opts o2 = o;
+    o2.rp_mode = MISTIC_RP_PCA;
+    select_reference_points(o2, d, na, mean, mn, mx, cov, pca);  // far points on one side of each axis
+  }
+  std::vector<double> cand;
+  for (uint32_t a = 0; a < na; ++a) {
+    const double* p = &pca[(size_t)a * d];
+    for (int side = 0; side < 2; ++side)
+      for (uint32_t i = 0; i < d; ++i) cand.push_back(side == 0 ? p[i] : 2.0 * mean[i] - p[i]);
+  }
+  SplitMix rng(o.seed ^ 0x73636f7265647270ull);
+  for (int c = 0; c < 8 && S > 0; ++c) {
+    const uint32_t r = (uint32_t)(rng.next() % S);
+    for (uint32_t i = 0; i < d; ++i) cand.push_back(sample[(size_t)r * d + i]);
+  }
+  for (int c = 0; c < 8; ++c)
+    for (uint32_t i = 0; i < d; ++i) cand.push_back(mn[i] + (mx[i] - mn[i]) * rng.uniform());
+  const uint32_t C = (uint32_t)(cand.size() / d);
+  // scoring sample: up to 1024 of the sample rows, evenly spaced
+  const uint32_t T = std::min<uint32_t>(S, 1024);
+  std::vector<uint32_t> rows(T);
+  for (uint32_t t = 0; t < T; ++t) rows[t] = (uint32_t)((uint64_t)t * S / std::max(1u, T));
+  const double w = eps > 0 ? eps : 1.0;
+  std::vector<int64_t> fld((size_t)C * T);
+  for (uint32_t c = 0; c < C; ++c)
+    for (uint32_t t = 0; t < T; ++t) {
+      const double* x = &sample[(size_t)rows[t] * d];
+      const double* r = &cand[(size_t)c * d];
+      double s2 = 0;
+      for (uint32_t i = 0; i < d; ++i) s2 += (x[i] - r[i]) * (x[i] - r[i]);
+      fld[(size_t)c * T + t] = (int64_t)std::floor(std::sqrt(s2) / w);
+    }
+  // surviving sample pairs (a < b), as a flat bitmap
+  const size_t NP = (size_t)T * (T - (T > 0)) / 2;
+  std::vector<uint8_t> alive(NP, 1);
+  std::vector<uint8_t> used(C, 0);
+  for (uint32_t j = 0; j < k; ++j) {
+    uint32_t best = UINT32_MAX;
+    size_t best_n = SIZE_MAX;
+    for (uint32_t c = 0; c < C; ++c) {
+      if (used[c]) continue;
+      const int64_t* f = &fld[(size_t)c * T];
+      size_t cnt = 0, pi = 0;
+      for (uint32_t a = 0; a < T; ++a)
+        for (uint32_t b = a + 1; b < T; ++b, ++pi)
+          if (alive[pi] && std::llabs(f[a] - f[b]) <= 1) ++cnt;
+      if (cnt < best_n) {
+        best_n = cnt;
+        best = c;
+      }
+    }
+    if (best == UINT32_MAX) break;
+    used[best] = 1;
+    const int64_t* f = &fld[(size_t)best * T];
+    size_t pi = 0;
+    for (uint32_t a = 0; a < T; ++a)
+      for (uint32_t b = a + 1; b < T; ++b, ++pi)
+        if (alive[pi] && std::llabs(f[a] - f[b]) > 1) alive[pi] = 0;
+    for (uint32_t i = 0; i < d; ++i) rps[(size_t)j * d + i] = cand[(size_t)best * d + i];
+  }
+}
+
 }  // namespace mistic

@@ -21,7 +21,7 @@ __all__ = ["MisticError", "JoinResult", "Handle", "selfjoin", "read_points", "co
 
 MODES = {"auto": L.MODE_AUTO, "fp64": L.MODE_FP64, "fp32": L.MODE_FP32, "bf16": L.MODE_BF16,
          "tf32": L.MODE_TF32}
-RP_MODES = {"pca": L.RP_PCA, "box": L.RP_BOX, "user": L.RP_USER}
+RP_MODES = {"pca": L.RP_PCA, "box": L.RP_BOX, "user": L.RP_USER, "scored": L.RP_SCORED}
 
 
 class MisticError(RuntimeError):

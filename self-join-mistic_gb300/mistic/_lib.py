@@ -21,7 +21,7 @@ ERR_NOT_FINITE, ERR_PAIR_OVERFLOW, ERR_TIMEOUT, ERR_NO_DEVICE = 5, 6, 7, 8
 ERR_IO, ERR_INTERNAL = 9, 10
 F64, F32 = 0, 1
 MODE_AUTO, MODE_FP64, MODE_FP32, MODE_BF16, MODE_TF32 = 0, 1, 2, 3, 4
-RP_PCA, RP_BOX, RP_USER = 0, 1, 2
+RP_PCA, RP_BOX, RP_USER, RP_SCORED = 0, 1, 2, 3
 PAIRS_NONE, PAIRS_HOST, PAIRS_DEVICE = 0, 1, 2
 
 #: every symbol include/mistic.h declares

@@ -52,7 +52,7 @@ def test_c1_full_size(handle, golden_full, mode):
     assert r.ulp_ambiguous == c["ulp_ambiguous"]
 
 
-@pytest.mark.parametrize("rp", ["pca", "box"])
+@pytest.mark.parametrize("rp", ["pca", "box", "scored"])
 @pytest.mark.parametrize("k", [1, 3, 6, 8, 16])
 def test_reference_point_choices_agree(handle, rp, k):
     rng = np.random.default_rng(100 + k)
@@ -61,6 +61,19 @@ def test_reference_point_choices_agree(handle, rp, k):
     ref = O.brute_pairs(x, eps)
     r = run(handle, x, k, eps, rp=rp)
     assert np.array_equal(r.pairs, ref), diff_pairs(r.pairs, ref)
+
+
+def test_scored_reference_points_prune_like_the_reference(handle):
+    """The reference's per-layer scoring (MISTIC_RP_SCORED): exact pair set,
+    and no more candidate pairs than seeded box points leave."""
+    from mistic import workloads as W
+    x = W.gen_susy_like(40000, seed=12)
+    eps = 0.03
+    ref = O.brute_pairs(x, eps)
+    scored = run(handle, x, 6, eps, rp="scored")
+    box = run(handle, x, 6, eps, rp="box")
+    assert np.array_equal(scored.pairs, ref), diff_pairs(scored.pairs, ref)
+    assert scored.candidates <= box.candidates
 
 
 def test_user_reference_points(handle):
