@@ -90,9 +90,9 @@ WORKLOADS = {
 FALLBACK_PEAKS = {"hbm_gbs": 6785.9, "bf16_tflops": 1922.1, "bf16_tflops_sustained": 1711.2}
 
 #: DRAM bytes (read + write) per evaluated cell of k_join_tc on the SUSY-shaped
-#: data, from an ncu capture of the 2.5M-point case (283.8 MB over 2.1993e10
+#: data, from an ncu capture of the 2.5M-point case (281.4 MB over 2.1546e10
 #: cells); scaled by the cells of the measured launch.
-TC_DRAM_BYTES_PER_CELL_SUSY18 = 283.8e6 / 2.1993e10
+TC_DRAM_BYTES_PER_CELL_SUSY18 = 281.4e6 / 2.1546e10
 
 
 def load_peaks() -> dict:
@@ -430,8 +430,9 @@ def run_mistic(args, wl) -> None:
                                       "same kernel x this launch's cells")
     else:
         # dominant kernel: the FP32 filter join; 3*d flops per candidate pair
-        # (d subtractions, d multiply-adds) on the CUDA-core FP32 pipe
-        work = r.candidates * 3.0 * d
+        # (d subtractions, d multiply-adds) on the CUDA-core FP32 pipe, over
+        # the candidate pairs it evaluated (those the tensor cores did not)
+        work = max(0, r.candidates - r.tc_cells) * 3.0 * d
         achieved = work / (simt_ms * 1e-3) / 1e12
         roof = {"bound": "fp32", "kernel": "k_join_f32r" if d <= 32 else "k_join_f32", "achieved": achieved,
                 "peak": fp32_peak,
