@@ -242,6 +242,7 @@ struct mistic_handle_s {
   cudaEvent_t ev[16] = {};
   cudaEvent_t jev[4] = {};  // around the two join kernels
   uint32_t launches = 0;
+  bool host_reads = false;  // kernels may read pageable host memory (coherent CPU-GPU link, host page tables)
   std::vector<mistic_handle_s*> workers;  // batch workers: own streams, same device (created on demand)
   cudaEvent_t batch_ev = nullptr;         // orders the workers' streams after this handle's stream
 };
