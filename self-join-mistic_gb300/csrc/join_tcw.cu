@@ -14,11 +14,13 @@
 // Unlike the short-row kernel (join_tc.cu) nothing is converted inside the
 // join: operands stream from L2 into shared memory in K chunks of 32.  The
 // home rows (contiguous) come as 128-row TMA tiles (cp.async.bulk.tensor,
-// 64-byte rows, 64B swizzle); the candidate rows, which come from several
-// bins, by cp.async in 16-byte chunks written to the same swizzled layout
-// (the MMAs ran 25% faster on it than on no-swizzle core matrices).  TMA
-// 4-row gathers of the candidate rows were measured slower: 64-byte rows
-// keep the copy engine busy far longer than the MMAs take.
+// 64-byte rows, 64B swizzle); so do a group's candidate rows when they are
+// one contiguous run of sorted rows (inside a large bin, or across bins that
+// follow one another).  Candidates from scattered bins come by cp.async in
+// 16-byte chunks written to the same swizzled layout (the MMAs ran 25% faster
+// on it than on no-swizzle core matrices).  TMA 4-row gathers of scattered
+// candidate rows were measured slower: 64-byte rows keep the copy engine busy
+// far longer than the MMAs take.
 //
 // Tiles: 2 home chunks of 128 rows (MMA M = 128 each) x up to 256 candidate
 // columns (MMA N), i.e. two 128 x 256 FP32 accumulators = all 512 TMEM
@@ -126,6 +128,20 @@ struct WShared {
 };
 
 __device__ __forceinline__ void wprod_sync() { asm volatile("bar.sync 1, %0;" ::"n"(WNPROD) : "memory"); }
+
+// wprod_sync that also returns the AND of p over all producer threads
+__device__ __forceinline__ bool wprod_sync_and(bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred pi, po;\n\t"
+      "setp.ne.u32 pi, %1, 0;\n\t"
+      "bar.red.and.pred po, 1, %2, pi;\n\t"
+      "selp.u32 %0, 1, 0, po;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)p), "n"(WNPROD)
+      : "memory");
+  return r != 0u;
+}
 
 // The tensor maps over the split rows (hi, lo): home-row tiles of 128 rows x
 // 32 bf16, 64B swizzle.
@@ -260,9 +276,10 @@ __global__ void k_tf32_rows(const float* __restrict__ xf, uint32_t dpad32, uint3
 // One persistent CTA per SM: 8 producer warps, 16 epilogue warps, 1 MMA warp.
 //   producers  fetch units; per group of up to 256 candidates all 8 warps
 //              compute the columns' sorted positions, ids, norms and
-//              thresholds; warp 0 then issues, per K chunk, the stage's TMA
-//              copies (home tiles + candidate gathers) against one
-//              expect_tx on the stage's full barrier;
+//              thresholds; then, per K chunk, thread 0 issues the stage's
+//              TMA tiles (home rows, and the candidate rows of a contiguous
+//              group) against one expect_tx on afull, and every producer
+//              thread copies its scattered candidate rows by cp.async;
 //   MMA warp   one lane issues 2 x 3 tcgen05.mma (K 16, M 128, N up to 256)
 //              per home chunk and stage, commits each stage to sfree and, at
 //              a group's last stage, each accumulator to dfull;
@@ -271,7 +288,7 @@ __global__ void k_tf32_rows(const float* __restrict__ xf, uint32_t dpad32, uint3
 //              to the pair list, the error band to the band list.
 // Barriers (all waits bounded by a %globaltimer deadline):
 //   full[s]   producers -> MMA       (WNPROD cp.async arrivals: candidate rows landed)
-//   afull[s]  producer 0 -> MMA      (one arrive.expect_tx + the TMA bytes of the home tiles)
+//   afull[s]  producer 0 -> MMA      (one arrive.expect_tx + the bytes of the stage's TMA tiles)
 //   gready[x] producers -> MMA       (WNPROD arrivals: group slot x written)
 //   sfree[s]  MMA -> producers       (tcgen05.commit: stage s read)
 //   dfull[g]  MMA -> epilogue        (tcgen05.commit, or a plain arrive to stop)
@@ -340,6 +357,13 @@ __global__ void __launch_bounds__(WTHREADS, 1)
       const uint32_t sl = pf++ & 1;
       if (tid == 0) S.pflag[sl] = wait_or_abort(b, parity, abort_flag, T.wait_limit) ? 1u : 0u;
       wprod_sync();
+      return S.pflag[sl] != 0u;
+    };
+    // the same, also returning the AND of p over the producers
+    auto shared_wait_and = [&](unsigned long long* b, uint32_t parity, bool p, bool* all) -> bool {
+      const uint32_t sl = pf++ & 1;
+      if (tid == 0) S.pflag[sl] = wait_or_abort(b, parity, abort_flag, T.wait_limit) ? 1u : 0u;
+      *all = wprod_sync_and(p);
       return S.pflag[sl] != 0u;
     };
     const uint16_t* XH = static_cast<const uint16_t*>(T.xh);
@@ -435,6 +459,20 @@ __global__ void __launch_bounds__(WTHREADS, 1)
           }
           q = S.w_start[lo] + (rank - S.w_pref[lo]);
         }
+        // the group's candidates are one contiguous run of sorted rows (the
+        // common case inside large bins) when every column sits at the first
+        // one's position + its index: then the stages fetch them as 128-row
+        // TMA tiles like the home rows
+        uint32_t qf;
+        {
+          int lo = 0, hi = (int)w_nb - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (S.w_pref[mid] <= w_pos) lo = mid; else hi = mid - 1;
+          }
+          qf = S.w_start[lo] + (w_pos - S.w_pref[lo]);
+        }
+        const bool in_run = !bcol || q == qf + t;
         float hqv = 0.f, dl = 0.f;
         uint32_t qid = 0;
         if (bcol) {
@@ -449,7 +487,8 @@ __global__ void __launch_bounds__(WTHREADS, 1)
           }
         }
         const uint32_t gs = group % WGS;
-        if (!shared_wait(&S.gfree[gs], ((group / WGS) & 1) ^ 1)) {
+        bool b_tma = false;
+        if (!shared_wait_and(&S.gfree[gs], ((group / WGS) & 1) ^ 1, in_run, &b_tma)) {
           aborted = true;
           break;
         }
@@ -503,7 +542,8 @@ __global__ void __launch_bounds__(WTHREADS, 1)
             b_src[i] = XS + ((size_t)qi * T.kd + 0) * ESZ + 16u * pch;
           if (prow0 + RSTEP * i < ncols) b_ok |= 1u << i;
         }
-        const uint32_t abytes = ng * 2u * A_CHUNK;  // = ng x 16 KB at every precision
+        const uint32_t nbt = b_tma ? (ncols + WM - 1) / WM : 0u;  // candidate tiles by TMA
+        const uint32_t abytes = (ng + nbt) * 2u * A_CHUNK;  // 16 KB a 128-row tile at every precision
         for (uint32_t kc = 0; kc < nkc; ++kc) {
           const uint32_t s = step % WNS;
           const long long cs0 = T.prof ? clock64() : 0;
@@ -524,8 +564,21 @@ __global__ void __launch_bounds__(WTHREADS, 1)
                 tma_tile_2d(sb + g * S_ACHUNK, map_ah, (int)(kc * KST), (int)(a0 + g * WM), ab);
               }
             }
+            // a contiguous group's candidate rows [qf, qf + 128 nbt): rows past
+            // ncols are fetched (or zero-filled past the last row) and never read
+            for (uint32_t b = 0; b < nbt; ++b) {
+              const int y = (int)(qf + b * WM);
+              if (PREC == 0) {
+                tma_tile_2d(sb + B_HI + b * A_CHUNK, map_ah, (int)(kc * WKC), y, ab);
+                tma_tile_2d(sb + B_LO + b * A_CHUNK, map_al, (int)(kc * WKC), y, ab);
+              } else {
+                tma_tile_2d(sb + S_B + b * S_ACHUNK, map_ah, (int)(kc * KST), y, ab);
+              }
+            }
           }
-          if (PREC == 0) {
+          if (b_tma) {
+            // fetched above
+          } else if (PREC == 0) {
             const uint32_t bdst = sb + (ph ? B_LO : B_HI);
 #pragma unroll
             for (int j = 0; j < WKC / 16; ++j) {
