@@ -38,7 +38,12 @@ struct PairStage {
   unsigned long long* buf;  // this warp's PSTAGE slots in shared memory
   uint32_t n;               // staged pairs (warp-uniform)
   uint32_t inst = 0;        // instance of the staged pairs (fused batch joins), or unit tag (pair ring)
+  bool ij = false;          // store pairs in the result's memory order (i, j) rather than packed
 };
+
+// A packed pair (i << 32 | j) in the result's memory order: i then j as two
+// uint32 (little-endian), i.e. the halves swapped.
+__device__ __forceinline__ unsigned long long pair_ij(unsigned long long v) { return (v >> 32) | (v << 32); }
 
 __device__ __forceinline__ uint32_t stage_scan(uint32_t x) {
   const int lane = threadIdx.x & 31;
@@ -116,7 +121,7 @@ __device__ __forceinline__ void stage_pairs(PairStage& ps, uint32_t cnt, F pair_
       unsigned long long pos = base + incl - cnt;
       for (uint32_t k = 0; k < cnt; ++k, ++pos)
         if (pos < cap) {
-          if (fits) pairs[pos] = pair_of(k);
+          if (fits) pairs[pos] = ps.ij ? pair_ij(pair_of(k)) : pair_of(k);
           if (rc) rc->tags[pos] = fits ? inst : RING_INVALID;
         }
     }
@@ -125,7 +130,7 @@ __device__ __forceinline__ void stage_pairs(PairStage& ps, uint32_t cnt, F pair_
   }
   if (pairs) {
     uint32_t pos = ps.n + incl - cnt;
-    for (uint32_t k = 0; k < cnt; ++k) ps.buf[pos + k] = pair_of(k);
+    for (uint32_t k = 0; k < cnt; ++k) ps.buf[pos + k] = ps.ij ? pair_ij(pair_of(k)) : pair_of(k);
   }
   __syncwarp();
   ps.n += total;

@@ -161,6 +161,7 @@ struct JoinParams {
   double amb;           // 4 ulp(eps2)
   unsigned long long* pairs;  // packed (i << 32 | j), i < j; null when counting only
   unsigned long long cap;
+  int pairs_ij;               // non-zero: pairs are stored in memory order (i, j) instead (pair_ij)
   unsigned long long* band_list;  // packed (i << 32 | j) original ids whose fast value is inside the error band
   unsigned long long band_cap;
   JoinCounters* ctr;
@@ -243,6 +244,8 @@ struct mistic_handle_s {
   cudaEvent_t jev[4] = {};  // around the two join kernels
   uint32_t launches = 0;
   bool host_reads = false;  // kernels may read pageable host memory (coherent CPU-GPU link, host page tables)
+  bool host_pairs = false;  // join kernels may write host pair lists into pinned host memory (same link)
+  unsigned long long host_pair_cap = 0;  // largest such host pair list so far (pairs)
   std::vector<mistic_handle_s*> workers;  // batch workers: own streams, same device (created on demand)
   cudaEvent_t batch_ev = nullptr;         // orders the workers' streams after this handle's stream
 };

@@ -310,7 +310,7 @@ k_join_f32(const JoinParams P) {
   const uint32_t nq4 = P.dpad >> 2;
   float4* sA = smem_f4 + (size_t)w * CH * nq4;
   unsigned long long* stg = reinterpret_cast<unsigned long long*>(smem_f4 + (size_t)(blockDim.x >> 5) * CH * nq4);
-  PairStage ps{stg + (size_t)w * PSTAGE, 0};
+  PairStage ps{stg + (size_t)w * PSTAGE, 0, 0, P.pairs_ij != 0};
   PairStage bs{stg + (size_t)((blockDim.x >> 5) + w) * PSTAGE, 0};
   const RingPair RP = ring_ctx(P);
   const RingCtx* rcp = P.ring ? &RP.pairs : nullptr;
@@ -373,7 +373,7 @@ k_join_f32r(const JoinParams P) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   float4* sA = smem_f4r + (size_t)w * CH * DQ;
   unsigned long long* stg = reinterpret_cast<unsigned long long*>(smem_f4r + (size_t)(blockDim.x >> 5) * CH * DQ);
-  PairStage ps{stg + (size_t)w * PSTAGE, 0};
+  PairStage ps{stg + (size_t)w * PSTAGE, 0, 0, P.pairs_ij != 0};
   PairStage bs{stg + (size_t)((blockDim.x >> 5) + w) * PSTAGE, 0};
   const RingPair RP = ring_ctx(P);
   const RingCtx* rcp = P.ring ? &RP.pairs : nullptr;
@@ -493,7 +493,8 @@ k_join_f64(const JoinParams P) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t nq2 = P.dpad >> 1;
   double2* sA = smem_d2 + (size_t)w * CH * nq2;
-  PairStage ps{reinterpret_cast<unsigned long long*>(smem_d2 + (size_t)(blockDim.x >> 5) * CH * nq2) + (size_t)w * PSTAGE, 0};
+  PairStage ps{reinterpret_cast<unsigned long long*>(smem_d2 + (size_t)(blockDim.x >> 5) * CH * nq2) + (size_t)w * PSTAGE, 0,
+               0, P.pairs_ij != 0};
   uint32_t amb_cnt = 0;
   const RingPair RP = ring_ctx(P);
   const RingCtx* rcp = P.ring ? &RP.pairs : nullptr;
@@ -624,7 +625,7 @@ __global__ void __launch_bounds__(256) k_band_check(const JoinParams P) {
       if (acc && P.pairs) {
         const unsigned long long pos = base + __popc(m & ((1u << lane) - 1u));
         if (pos < P.cap) {
-          P.pairs[pos] = e;
+          P.pairs[pos] = P.pairs_ij ? pair_ij(e) : e;
           if (P.ring) P.pair_tags[pos] = tag;
         }
       }

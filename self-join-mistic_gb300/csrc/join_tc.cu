@@ -1078,7 +1078,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
     // accumulator
     const uint32_t quarter = warp & 3;
     const uint32_t cblk0 = (warp - EPI0) >> 2;
-    PairStage ps{pstage + (warp - EPI0) * PSTAGE, 0};
+    PairStage ps{pstage + (warp - EPI0) * PSTAGE, 0, 0, P.pairs_ij != 0};
     PairStage bs{pstage + (NEPI + warp - EPI0) * PSTAGE, 0};
     const RingCtx rcp_{P.pair_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
     const RingCtx rcb_{P.band_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
@@ -1109,10 +1109,19 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         tmem_wait();
         if (T.prof) ec_ld += clock64() - cl0;
         // sign bits (D' < 0: a candidate), column c0 + j at bit j: one
-        // funnel shift per value
-        uint32_t m = 0;
+        // funnel shift per value, in four independent chains of 8
+        uint32_t m;
+        {
+          uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
 #pragma unroll
-        for (int j = 31; j >= 0; --j) m = __funnelshift_l(v[j], m, 1);
+          for (int j = 7; j >= 0; --j) {
+            m0 = __funnelshift_l(v[j], m0, 1);
+            m1 = __funnelshift_l(v[8 + j], m1, 1);
+            m2 = __funnelshift_l(v[16 + j], m2, 1);
+            m3 = __funnelshift_l(v[24 + j], m3, 1);
+          }
+          m = m0 | (m1 << 8) | (m2 << 16) | (m3 << 24);
+        }
         const uint32_t nvalid = min(32u, M.ncols - c0);
         if (nvalid < 32) m &= (1u << nvalid) - 1u;
         if (!row_ok) m = 0;

@@ -809,7 +809,7 @@ __global__ void __launch_bounds__(WTHREADS, 1)
     // the 32-column blocks (w - WEPI0) / 4, + 2, + 4, ... of each accumulator
     const uint32_t quarter = warp & 3;
     const uint32_t cblk0 = (warp - WEPI0) >> 2;
-    PairStage ps{pstage + (warp - WEPI0) * PSTAGE, 0};
+    PairStage ps{pstage + (warp - WEPI0) * PSTAGE, 0, 0, P.pairs_ij != 0};
     PairStage bs{pstage + (WNEPI + warp - WEPI0) * PSTAGE, 0};
     const RingCtx rcp_{P.pair_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};
     const RingCtx rcb_{P.band_tags, P.deferred, P.def_out, &P.ctr->def_n, &P.ctr->stop};

@@ -211,6 +211,16 @@ PinnedCache& pinned_cache() {
   return *c;
 }
 
+// A pinned block owned by a call until it is handed to the result.
+struct PinnedHold {
+  void* p = nullptr;
+  void reset() {
+    if (p) pinned_cache().release(p);
+    p = nullptr;
+  }
+  ~PinnedHold() { reset(); }
+};
+
 template <class T>
 T* abuf(mistic_handle_s* h, const char* name, size_t count) {
   return (T*)h->arena.get(name, count * sizeof(T));
@@ -1370,6 +1380,21 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   unsigned long long cap = 0;
   unsigned long long* pbuf = nullptr;
   const bool caller_buf = want_pairs && o.pairs == MISTIC_PAIRS_DEVICE && o.pair_buffer;
+  // A host pair list that needs no device-side pass (no sort, no CSR table)
+  // is written by the join kernels straight into pinned host memory where the
+  // CPU-GPU link is coherent: the stores cross the link while the join runs,
+  // in the result's (i, j) order, and no copy follows the join.
+  bool host_direct = want_pairs && o.pairs == MISTIC_PAIRS_HOST && !o.sort_pairs && !want_csr && h->host_pairs;
+  PinnedHold hold;
+  auto host_list = [&](unsigned long long c) -> unsigned long long* {
+    hold.reset();
+    hold.p = pinned_cache().acquire(std::max<size_t>(8, c * 8));
+    void* dp = nullptr;
+    if (hold.p && cudaHostGetDevicePointer(&dp, hold.p, 0) == cudaSuccess) return (unsigned long long*)dp;
+    cudaGetLastError();
+    hold.reset();
+    return nullptr;
+  };
   if (caller_buf) {
     if (!o.pair_capacity) throw Error(MISTIC_ERR_INVALID_ARG, "pair_buffer needs pair_capacity > 0");
     if ((uintptr_t)o.pair_buffer % 8) throw Error(MISTIC_ERR_INVALID_ARG, "pair_buffer must be 8-byte aligned");
@@ -1377,12 +1402,20 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     pbuf = (unsigned long long*)o.pair_buffer;
   } else if (need_pairs) {
     cap = o.pair_capacity ? o.pair_capacity : std::max<unsigned long long>(1ull << 20, 16ull * n);
-    auto it = h->arena.bufs.find("pairs");
-    if (!o.pair_capacity && it != h->arena.bufs.end()) cap = std::max<unsigned long long>(cap, it->second.bytes / 8);
-    pbuf = abuf<unsigned long long>(h, "pairs", cap);
+    if (host_direct) {
+      if (!o.pair_capacity) cap = std::max<unsigned long long>(cap, h->host_pair_cap);
+      pbuf = host_list(cap);
+      host_direct = pbuf != nullptr;  // no pinned block: the device list and a copy
+    }
+    if (!host_direct) {
+      auto it = h->arena.bufs.find("pairs");
+      if (!o.pair_capacity && it != h->arena.bufs.end()) cap = std::max<unsigned long long>(cap, it->second.bytes / 8);
+      pbuf = abuf<unsigned long long>(h, "pairs", cap);
+    }
   }
   jp.pairs = pbuf;
   jp.cap = cap;
+  jp.pairs_ij = host_direct ? 1 : 0;
   size_band(totc);
   JoinCounters hc{};
   // MISTIC_TEST_JOIN_ATTEMPTS=k caps the passes (tests of the exit check below)
@@ -1403,9 +1436,14 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
       break;
     }
     cap = hc.pairs;
-    pbuf = abuf<unsigned long long>(h, "pairs", cap);
+    if (host_direct) {
+      pbuf = host_list(cap);
+      host_direct = pbuf != nullptr;
+    }
+    if (!host_direct) pbuf = abuf<unsigned long long>(h, "pairs", cap);
     jp.pairs = pbuf;
     jp.cap = cap;
+    jp.pairs_ij = host_direct ? 1 : 0;
   }
   // the last pass must have decided every band pair and, with a library-sized
   // pair buffer, stored every pair; otherwise the counts are not a result
@@ -1486,7 +1524,16 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
     }
   }
   // ---- pair list
-  if (want_pairs) {
+  if (want_pairs && host_direct) {
+    const unsigned long long stored = std::min<unsigned long long>(hc.pairs, cap);
+    if (hc.pairs > cap) tail = MISTIC_ERR_PAIR_OVERFLOW;
+    h->host_pair_cap = std::max(h->host_pair_cap, cap);
+    r->pairs = (uint32_t*)hold.p;  // the join's stores completed with its last kernel (synchronised above)
+    r->pairs_len = stored;
+    r->pairs_on_device = 0;
+    r->_owner = hold.p;
+    hold.p = nullptr;
+  } else if (want_pairs) {
     const unsigned long long stored = std::min<unsigned long long>(hc.pairs, cap);
     if (hc.pairs > cap) tail = MISTIC_ERR_PAIR_OVERFLOW;
     if (o.sort_pairs && stored > 1) {
@@ -2067,6 +2114,8 @@ mistic_status mistic_create(mistic_handle* out, int device, void* stream) {
       cudaGetLastError();
       const char* e = getenv("MISTIC_HOST_READS");  // 0: staging ring / plain copies only
       h->host_reads = pma && hpt && !(e && *e == '0');
+      const char* e2 = getenv("MISTIC_HOST_PAIRS");  // 0: host pair lists by a copy after the join
+      h->host_pairs = pma && hpt && !(e2 && *e2 == '0');
     }
     if (stream) {
       h->stream = (cudaStream_t)stream;
