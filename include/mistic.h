@@ -303,8 +303,8 @@ const char* mistic_last_error(mistic_handle h);
  * in it minus 256 bytes (e.g. n <= 419,427 at d = 18), and d must be at most
  * MISTIC_NOALLOC_MAX_D; larger inputs are rejected with MISTIC_ERR_TOO_LARGE.
  * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current: make it before any stream
- * capture.  Under CUDA's default lazy module loading the array is allocated
+ * (cudaGetSymbolAddress) with that device current.  Under CUDA's default
+ * lazy module loading the array is allocated
  * when the library's module first loads on the device, which is that first
  * call: make it before a pool allocator reserves the device's memory (a call
  * with n = 0 does only this set-up).  Inputs with a NaN or infinite

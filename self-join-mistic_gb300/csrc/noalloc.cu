@@ -22,8 +22,7 @@
 // GPU can reach host memory, silently use the wrong memory.  So the first
 // call on each device looks the device address up with cudaGetSymbolAddress
 // (with that device current), checks the result and caches it; kernels get
-// that pointer.  Make the first call on a device before any stream capture.
-// Under CUDA's default lazy module loading the array itself is only
+// that pointer.  Under CUDA's default lazy module loading the array itself is only
 // allocated when this module first loads on a device, i.e. at that first
 // call: make it (a call with n = 0 does only the set-up) before a pool
 // allocator reserves the device's memory.
