@@ -193,7 +193,7 @@ class PinnedCache {
   }
 
  private:
-  static constexpr size_t kMaxCached = 8ull << 30;
+  static constexpr size_t kMaxCached = 12ull << 30;
   static size_t size_class(size_t bytes) {
     if (bytes <= (1u << 16)) return 1u << 16;
     int lg = 63 - __builtin_clzll((unsigned long long)bytes);
@@ -246,6 +246,8 @@ constexpr size_t kStageSlotBytes = 8u << 20;
 constexpr int kStageThreads = 8;
 constexpr int kStageSlots = 2 * kStageThreads;
 constexpr size_t kStageMin = 128u << 20;
+// below this a plain copy costs about what a kernel launch does
+constexpr size_t kHostReadMin = 64u << 10;
 static_assert(kStageSlots <= (int)(sizeof(((mistic_handle_s*)nullptr)->stage_ev) / sizeof(cudaEvent_t)),
               "one event per staging slot");
 
@@ -260,13 +262,15 @@ __global__ void k_copy_from_host(const uint4* __restrict__ src, uint4* __restric
 // (GB300 with a Grace host: coherent NVLink-C2C and the host's page tables),
 // one kernel pulls the caller's array straight into HBM: 720 MB in 3.8 ms,
 // the link's rate, against 9 ms through the staging ring below, which pays
-// a host memcpy into pinned slots.  Elsewhere inputs of 128 MB or more go
-// through that ring, smaller ones through one plain copy.
+// a host memcpy into pinned slots.  The kernel also serves inputs down to
+// 64 KB, which a plain pageable copy moves at a few GB/s (the instances of a
+// batch).  Elsewhere inputs of 128 MB or more go through that ring, smaller
+// ones through one plain copy.
 void h2d(mistic_handle_s* h, void* dst, const void* src, size_t bytes) {
-  if (bytes >= kStageMin && h->host_reads && (uintptr_t)src % 16 == 0 && (uintptr_t)dst % 16 == 0) {
+  if (bytes >= kHostReadMin && h->host_reads && (uintptr_t)src % 16 == 0 && (uintptr_t)dst % 16 == 0) {
     const size_t n16 = bytes / 16;
-    k_copy_from_host<<<(unsigned)(h->sms * 8), 256, 0, h->stream>>>(static_cast<const uint4*>(src),
-                                                                    static_cast<uint4*>(dst), n16);
+    const unsigned grid = (unsigned)std::min<size_t>((size_t)h->sms * 8, (n16 + 255) / 256);
+    k_copy_from_host<<<grid, 256, 0, h->stream>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), n16);
     launched(h, "copy_from_host");
     if (bytes % 16)
       MCK(cudaMemcpyAsync(static_cast<unsigned char*>(dst) + n16 * 16, static_cast<const unsigned char*>(src) + n16 * 16,
@@ -1946,28 +1950,21 @@ mistic_status run_batch_fused(mistic_handle h, const mistic_instance* inst, uint
     if (pstart[G] != hc.pairs) throw Error(MISTIC_ERR_INTERNAL, "per-instance pair counts do not add up");
     k_localize<<<(unsigned)((hc.pairs + 255) / 256), 256, 0, h->stream>>>(sorted, hc.pairs, d_row0, G);
     launched(h, "localize");
-    unsigned long long* host_all = nullptr;
-    if (o.pairs == MISTIC_PAIRS_HOST) {
-      host_all = (unsigned long long*)malloc(hc.pairs * 8);
-      if (!host_all) throw Error(MISTIC_ERR_OUT_OF_MEMORY, "host pair buffer");
-      MCK(cudaMemcpyAsync(host_all, sorted, hc.pairs * 8, cudaMemcpyDeviceToHost, h->stream));
-    }
-    MCK(cudaStreamSynchronize(h->stream));
     for (uint32_t g = 0; g < G; ++g) {
       mistic_result& r = results[gl[g]];
       const unsigned long long np = ipairs[g];
       r.pairs_len = np;
       if (o.pairs == MISTIC_PAIRS_HOST) {
+        // each instance's slice of the sorted list straight into its own
+        // pinned block (a staging copy through one pageable array cost two
+        // passes over the host memory of every pair)
         uint32_t* hp = (uint32_t*)pinned_cache().acquire(std::max<size_t>(1, np * 8));
         if (!hp) hp = (uint32_t*)malloc(std::max<size_t>(1, np * 8));
-        if (!hp) {
-          free(host_all);
-          throw Error(MISTIC_ERR_OUT_OF_MEMORY, "host pair buffer");
-        }
-        memcpy(hp, host_all + pstart[g], np * 8);
+        if (!hp) throw Error(MISTIC_ERR_OUT_OF_MEMORY, "host pair buffer");
         r.pairs = hp;
         r.pairs_on_device = 0;
         r._owner = hp;
+        if (np) MCK(cudaMemcpyAsync(hp, sorted + pstart[g], np * 8, cudaMemcpyDeviceToHost, h->stream));
       } else {
         void* dp = nullptr;
         MCK(cudaMalloc(&dp, std::max<size_t>(8, np * 8)));
@@ -1977,7 +1974,6 @@ mistic_status run_batch_fused(mistic_handle h, const mistic_instance* inst, uint
         r._owner = dp;
       }
     }
-    free(host_all);
     MCK(cudaStreamSynchronize(h->stream));
   }
   const double wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
