@@ -745,6 +745,20 @@ def run_batch(args) -> None:
                "sample": f"row samples of 8 instances ({t_s:.1f} s), scaled by sum n^2 d to all {m}; "
                          "brute_force of src/utils.cu:285-317 (oracle C port, OpenMP)"}
     pairs = sum(p[0] for p in res)
+    # the whole fused step against the tensor peak: 2*d flops per candidate
+    # pair, summed over the instances (their joins run on the short-row
+    # tensor-core kernel and the FP32 filter, so the FP32 CUDA-core peak is
+    # given beside it)
+    peaks = load_peaks()
+    work = sum(2.0 * x.shape[1] * p[2] for x, p in zip(xs, res))
+    achieved = work / (ms * 1e-3) / 1e12
+    fp32_peak = measure_fp32_peak()
+    roof = {"bound": "tensor", "kernel": "fused batch join (all join kernels of the step)", "achieved": achieved,
+            "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"],
+            "traffic": None, "work": "2*d flops per candidate pair, summed over the instances; whole step time",
+            "peak_source": peaks["_source"] + " bf16 burst (of measured)",
+            "fp32_simt_peak_tflops": fp32_peak,
+            "frac_of_fp32_simt": achieved / fp32_peak if fp32_peak else None}
     line = {
         "metric": METRIC, "value": world * tot_n / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -763,7 +777,7 @@ def run_batch(args) -> None:
         "fused_vs_serial": serial_ms / ms, "fused_vs_streams": streams_ms / ms,
         "counts_identical_fused_vs_per_instance": counts_same,
         "generation_s": t_gen, "parity": parity,
-        "roofline": None,
+        "roofline": roof,
         "e2e": {"value": world * tot_n / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": sum(x.nbytes for x in xs), "d2h_bytes_per_step": pairs * 8},
         "gpu_launches": sum(p[1] for p in res),

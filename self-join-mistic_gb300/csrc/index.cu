@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(128, 8) k_enum(const uint64_t* __restrict__ bk
   auto leaf = [&](uint32_t a) {
     const uint32_t bsz = bstart[a + 1] - bstart[a];
     c += (a == hb) ? self_s : rows_s * bsz;
-    if (seg_fill > 0 && seg_fill + bsz > P.seg_cap) {
+    if (seg_fill > 0 && seg_fill + bsz > (tc ? P.seg_cap_tc : P.seg_cap)) {
       if (FILL) {
         for (uint32_t ch = 0; ch < nchunks; ++ch)
           if (group_sampled(hb, ch * csz / SAMPLE_GROUP, P.sample))

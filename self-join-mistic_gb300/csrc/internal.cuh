@@ -102,7 +102,8 @@ struct EnumParams {
   int k;
   int shift[MAX_K];
   uint32_t maxkey[MAX_K];
-  uint32_t seg_cap;  // candidate points per neighbour segment
+  uint32_t seg_cap;     // candidate points per neighbour segment (CUDA-core units)
+  uint32_t seg_cap_tc;  // the same for tensor-core units
   uint32_t chunk;    // home points per CUDA-core unit
   uint32_t tc_min;   // home bins with at least this many points get tensor-core units (0: none)
   uint32_t tc_chunk; // home points per tensor-core unit

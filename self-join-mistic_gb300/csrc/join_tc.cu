@@ -335,8 +335,8 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
     // costs (finding its source row, issuing its copies, its threshold and
     // metadata) are paid once.  Pairs never span a window of neighbour bins:
     // when fewer than 129 candidate ranks are left in it, the pair is one
-    // tile and group 1 idles.  Up to two pairs are in flight (one raw slot a
-    // tile).  Branches that lead to bar.sync depend only on values every
+    // tile and group 1 idles.  Two pairs are in flight, the one being
+    // converted and the next (one raw slot a tile).  Branches that lead to bar.sync depend only on values every
     // producer thread holds or reads after the same bar.sync; barrier waits
     // are done by thread 0 and broadcast through S.pflag.
     const uint32_t pr = (uint32_t)tid & 127u, grp = (uint32_t)tid >> 7;
@@ -543,15 +543,18 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
         return 1;
       };
 
+      // One pair is in flight ahead of the pair being converted.  The next
+      // pair's copies and home-column entries are issued only after the
+      // barrier that ends every thread's work on the pair before it, whose
+      // raw slots and entries they reuse: a pair of one tile shifts the slots
+      // by one, so the thread that converted a slot is not always the thread
+      // that refills it.
       bool first = true, aborted = false;
+      if (w_pos < w_total || seg_next < U.s1) advance();
       for (;;) {
-        while (pin < 2 && (w_pos < w_total || seg_next < U.s1)) advance();
         if (pin == 0) break;
         const long long cc0 = T.prof ? clock64() : 0;
-        if (pin == 2)
-          asm volatile("cp.async.wait_group 1;" ::: "memory");
-        else
-          asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
         if (T.prof) pc_ldw += clock64() - cc0;
         const uint32_t e = (uint32_t)(pq & 0x3ffffull);
         pq >>= 18;
@@ -575,6 +578,7 @@ __global__ void __launch_bounds__(tc_threads(NEPI), 1) k_join_tc(const JoinParam
           aborted = true;
           break;
         }
+        if (w_pos < w_total || seg_next < U.s1) advance();
         if (grp < nt) {
           const uint32_t mt = tile + grp;
           const uint32_t st = mt % NS, rs = mt % RAW;

@@ -573,27 +573,36 @@ bool tune_lookup(mistic_handle_s* h, const mistic_opts& o, uint32_t d, mistic_dt
   double best = 1e300;
   Tuned bt{cands[0].tc_min, cands[0].prec};
   const unsigned long long want_units = 20ull * (unsigned long long)h->sms;
-  for (size_t i = 0; i < cands.size(); ++i) {
-    double ms = 0;
-    unsigned long long cc = 0, uu = 0;
-    measure(cands[i], S, &ms, &cc, &uu);
-    if (i == 0) {
-      uint32_t S2 = S;
-      if (uu < want_units) S2 = (uint32_t)std::max(1.0, S * (double)uu / (double)want_units);
-      if (ms * S / S2 > 400.0) S2 = (uint32_t)std::min(4096.0, std::ceil(S * ms / 400.0));
-      if (S2 != S) {
-        S = S2;
-        measure(cands[i], S, &ms, &cc, &uu);
+  // two rounds, the second in reverse order, each candidate keeping its
+  // faster run: neighbouring thresholds differ by a few percent, about what
+  // one run of a sample varies
+  std::vector<double> t_best(cands.size(), 1e300);
+  for (int round = 0; round < 2; ++round) {
+    for (size_t j = 0; j < cands.size(); ++j) {
+      const size_t i = round == 0 ? j : cands.size() - 1 - j;
+      double ms = 0;
+      unsigned long long cc = 0, uu = 0;
+      measure(cands[i], S, &ms, &cc, &uu);
+      if (round == 0 && i == 0) {
+        uint32_t S2 = S;
+        if (uu < want_units) S2 = (uint32_t)std::max(1.0, S * (double)uu / (double)want_units);
+        if (ms * S / S2 > 400.0) S2 = (uint32_t)std::min(4096.0, std::ceil(S * ms / 400.0));
+        if (S2 != S) {
+          S = S2;
+          measure(cands[i], S, &ms, &cc, &uu);
+        }
       }
-    }
-    if (getenv("MISTIC_DEBUG"))
-      fprintf(stderr, "[mistic] tune %s: tc_min=%u prec=%d sample 1/%u: %.3f ms (%llu candidates)\n", key,
-              cands[i].tc_min, cands[i].prec, S, ms, cc);
-    if (ms < best) {
-      best = ms;
-      bt = Tuned{cands[i].tc_min, cands[i].prec};
+      if (getenv("MISTIC_DEBUG"))
+        fprintf(stderr, "[mistic] tune %s: tc_min=%u prec=%d sample 1/%u: %.3f ms (%llu candidates)\n", key,
+                cands[i].tc_min, cands[i].prec, S, ms, cc);
+      t_best[i] = std::min(t_best[i], ms);
     }
   }
+  for (size_t i = 0; i < cands.size(); ++i)
+    if (t_best[i] < best) {
+      best = t_best[i];
+      bt = Tuned{cands[i].tc_min, cands[i].prec};
+    }
   tune_cache().put(key, bt, best);
   *out = bt;
   return true;
@@ -915,6 +924,13 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   const int CH = join::chunk_for(fp64, fp64 ? dpad64 : dpad32);
   ep.chunk = (uint32_t)CH;
   ep.seg_cap = 4096;
+  // tensor-core units of large joins take longer segments: each unit reloads
+  // and converts its home rows and drains the tile pipeline once, which cost
+  // 4 ms of the 5M x 18 join at 4096 points against 16384; small joins keep
+  // short segments so that the persistent grid has units enough to balance,
+  // and the pair ring keeps them so that a unit's pairs fit it
+  ep.seg_cap_tc = (n >= (1u << 20) && o.ring_capacity == 0) ? 16384u : 4096u;
+  if (const char* e = getenv("MISTIC_SEG_CAP_TC")) ep.seg_cap_tc = (uint32_t)std::max(128l, strtol(e, nullptr, 10));
   ep.sample = o.home_sample;
   ep.tc_min = use_tc ? tc_min_bin(d, wide) : 0u;
   ep.tc_chunk = use_tc ? (wide ? 256u : join::tc_rows(d)) : 128;
