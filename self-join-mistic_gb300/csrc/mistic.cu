@@ -1123,7 +1123,11 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
           MCK(cudaEventElapsedTime(&t, h->jev[0], h->jev[3]));
           *ms_out = t;
           *cands = totc;
-          *nunits = (unsigned long long)tots[1] + tots[2];
+          // the sample must give each join enough units to balance the
+          // persistent grid (tensor-core units are long and few): the
+          // smaller of the two counts decides
+          const unsigned long long us = tots[1], ut = tots[2];
+          *nunits = (us && ut) ? std::min(us, ut) : us + ut;
         })) {
       ep.tc_min = tu.tc_min;
       prec_used = tu.prec;
