@@ -352,17 +352,19 @@ __global__ void __launch_bounds__(WTHREADS, 1)
     long long pc_grp = 0, pc_sfree = 0, pc_issue = 0, pc_pub = 0;  // cycles (T.prof)
     const long long p_start = T.prof ? clock64() : 0;
     const uint64_t map_ah = reinterpret_cast<uint64_t>(&M.ah), map_al = reinterpret_cast<uint64_t>(&M.al);
-    // thread 0 waits on b (bounded), all producers learn the outcome
+    // thread 0 waits on b (bounded), all producers learn the outcome; once
+    // the CTA aborts every such wait fails (thread 0 may have given up alone
+    // while issuing a contiguous group's stages)
     auto shared_wait = [&](unsigned long long* b, uint32_t parity) -> bool {
       const uint32_t sl = pf++ & 1;
-      if (tid == 0) S.pflag[sl] = wait_or_abort(b, parity, abort_flag, T.wait_limit) ? 1u : 0u;
+      if (tid == 0) S.pflag[sl] = (!*abort_flag && wait_or_abort(b, parity, abort_flag, T.wait_limit)) ? 1u : 0u;
       wprod_sync();
       return S.pflag[sl] != 0u;
     };
     // the same, also returning the AND of p over the producers
     auto shared_wait_and = [&](unsigned long long* b, uint32_t parity, bool p, bool* all) -> bool {
       const uint32_t sl = pf++ & 1;
-      if (tid == 0) S.pflag[sl] = wait_or_abort(b, parity, abort_flag, T.wait_limit) ? 1u : 0u;
+      if (tid == 0) S.pflag[sl] = (!*abort_flag && wait_or_abort(b, parity, abort_flag, T.wait_limit)) ? 1u : 0u;
       *all = wprod_sync_and(p);
       return S.pflag[sl] != 0u;
     };
@@ -544,6 +546,56 @@ __global__ void __launch_bounds__(WTHREADS, 1)
         }
         const uint32_t nbt = b_tma ? (ncols + WM - 1) / WM : 0u;  // candidate tiles by TMA
         const uint32_t abytes = (ng + nbt) * 2u * A_CHUNK;  // 16 KB a 128-row tile at every precision
+        if (b_tma) {
+          // every copy of the group's stages is a TMA tile: thread 0 alone
+          // waits for each stage, issues its tiles and makes all WNPROD
+          // arrivals on its full barrier; the other producers go on to the
+          // next group (whose slot barrier thread 0 joins when done).  A
+          // failed wait leaves the CTA's abort flag set, which fails the next
+          // shared wait of every producer.
+          if (tid == 0) {
+            for (uint32_t kc = 0; kc < nkc; ++kc) {
+              const uint32_t s = step % WNS;
+              const long long cs0 = T.prof ? clock64() : 0;
+              if (!wait_or_abort(&S.sfree[s], ((step / WNS) & 1) ^ 1, abort_flag, T.wait_limit)) break;
+              const long long cs1 = T.prof ? clock64() : 0;
+              const uint32_t sb = stage_base + s * STAGE_BYTES;
+              const uint32_t ab = smem_u32(&S.afull[s]);
+              mbar_expect_tx(ab, abytes);
+              for (uint32_t g = 0; g < ng; ++g) {
+                if (PREC == 0) {
+                  tma_tile_2d(sb + g * A_CHUNK, map_ah, (int)(kc * WKC), (int)(a0 + g * WM), ab);
+                  tma_tile_2d(sb + A_LO + g * A_CHUNK, map_al, (int)(kc * WKC), (int)(a0 + g * WM), ab);
+                } else {
+                  tma_tile_2d(sb + g * S_ACHUNK, map_ah, (int)(kc * KST), (int)(a0 + g * WM), ab);
+                }
+              }
+              // the candidate rows [qf, qf + 128 nbt): rows past ncols are
+              // fetched (or zero-filled past the last row) and never read
+              for (uint32_t b = 0; b < nbt; ++b) {
+                const int y = (int)(qf + b * WM);
+                if (PREC == 0) {
+                  tma_tile_2d(sb + B_HI + b * A_CHUNK, map_ah, (int)(kc * WKC), y, ab);
+                  tma_tile_2d(sb + B_LO + b * A_CHUNK, map_al, (int)(kc * WKC), y, ab);
+                } else {
+                  tma_tile_2d(sb + S_B + b * S_ACHUNK, map_ah, (int)(kc * KST), y, ab);
+                }
+              }
+              mbar_arrive_n(&S.full[s], WNPROD);
+              ++step;
+              if (T.prof) {
+                const long long cs2 = clock64();
+                pc_sfree += cs1 - cs0;
+                pc_issue += cs2 - cs1;
+              }
+            }
+          } else {
+            step += nkc;
+          }
+          w_pos += ncols;
+          ++group;
+          continue;
+        }
         for (uint32_t kc = 0; kc < nkc; ++kc) {
           const uint32_t s = step % WNS;
           const long long cs0 = T.prof ? clock64() : 0;
@@ -564,21 +616,8 @@ __global__ void __launch_bounds__(WTHREADS, 1)
                 tma_tile_2d(sb + g * S_ACHUNK, map_ah, (int)(kc * KST), (int)(a0 + g * WM), ab);
               }
             }
-            // a contiguous group's candidate rows [qf, qf + 128 nbt): rows past
-            // ncols are fetched (or zero-filled past the last row) and never read
-            for (uint32_t b = 0; b < nbt; ++b) {
-              const int y = (int)(qf + b * WM);
-              if (PREC == 0) {
-                tma_tile_2d(sb + B_HI + b * A_CHUNK, map_ah, (int)(kc * WKC), y, ab);
-                tma_tile_2d(sb + B_LO + b * A_CHUNK, map_al, (int)(kc * WKC), y, ab);
-              } else {
-                tma_tile_2d(sb + S_B + b * S_ACHUNK, map_ah, (int)(kc * KST), y, ab);
-              }
-            }
           }
-          if (b_tma) {
-            // fetched above
-          } else if (PREC == 0) {
+          if (PREC == 0) {
             const uint32_t bdst = sb + (ph ? B_LO : B_HI);
 #pragma unroll
             for (int j = 0; j < WKC / 16; ++j) {
@@ -656,7 +695,9 @@ __global__ void __launch_bounds__(WTHREADS, 1)
       uint32_t use[WG] = {0, 0};
       unsigned long long* last_bar = nullptr;
       uint32_t last_par = 0;
-      bool ok = true;
+      // failure-detection test: the lane signals nothing, so the producers'
+      // and the epilogue's bounded waits run out
+      bool ok = !T.stall_test;
       long long mw_full = 0, mw_dfree = 0;
       const long long m_start = T.prof ? clock64() : 0;
       while (ok) {

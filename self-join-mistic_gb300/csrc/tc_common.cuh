@@ -81,6 +81,11 @@ __device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count)
 __device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
   asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(smem_u32(b)) : "memory");
 }
+// n arrivals at once
+__device__ __forceinline__ void mbar_arrive_n(unsigned long long* b, uint32_t n) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0], %1;\n}" ::"r"(smem_u32(b)), "r"(n)
+               : "memory");
+}
 __device__ __forceinline__ void tc_commit(unsigned long long* b) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(b))
                : "memory");
