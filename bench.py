@@ -90,9 +90,9 @@ WORKLOADS = {
 FALLBACK_PEAKS = {"hbm_gbs": 6785.9, "bf16_tflops": 1922.1, "bf16_tflops_sustained": 1711.2}
 
 #: DRAM bytes (read + write) per evaluated cell of k_join_tc on the SUSY-shaped
-#: data, from an ncu capture of the 2.5M-point case (281.4 MB over 2.1546e10
+#: data, from an ncu capture of the 2.5M-point case (317.9 MB over 2.3567e10
 #: cells); scaled by the cells of the measured launch.
-TC_DRAM_BYTES_PER_CELL_SUSY18 = 281.4e6 / 2.1546e10
+TC_DRAM_BYTES_PER_CELL_SUSY18 = 317.9e6 / 2.3567e10
 
 
 def load_peaks() -> dict:

@@ -245,6 +245,12 @@ struct mistic_handle_s {
   cudaEvent_t jev[4] = {};  // around the two join kernels
   uint32_t launches = 0;
   bool host_reads = false;  // kernels may read pageable host memory (coherent CPU-GPU link, host page tables)
+  // large host-read copies (mistic::h2d): events around the last one and its
+  // size (0: none to check), and the large copies left to take through the
+  // staging ring after one that ran slower than the ring
+  cudaEvent_t hr_ev[2] = {};
+  size_t hr_bytes = 0;
+  uint32_t hr_skip = 0;
   bool host_pairs = false;  // join kernels may write host pair lists into pinned host memory (same link)
   unsigned long long host_pair_cap = 0;  // largest such host pair list so far (pairs)
   std::vector<mistic_handle_s*> workers;  // batch workers: own streams, same device (created on demand)

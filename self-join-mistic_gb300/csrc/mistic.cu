@@ -267,11 +267,43 @@ __global__ void k_copy_from_host(const uint4* __restrict__ src, uint4* __restric
 // batch).  Elsewhere inputs of 128 MB or more go through that ring, smaller
 // ones through one plain copy.
 void h2d(mistic_handle_s* h, void* dst, const void* src, size_t bytes) {
-  if (bytes >= kHostReadMin && h->host_reads && (uintptr_t)src % 16 == 0 && (uintptr_t)dst % 16 == 0) {
+  bool kernel = bytes >= kHostReadMin && h->host_reads && (uintptr_t)src % 16 == 0 && (uintptr_t)dst % 16 == 0;
+  bool timed = false;
+  if (kernel && bytes >= kStageMin) {
+    // The kernel usually reads at the link's rate (about 200 GB/s), but on
+    // some machines and in some processes the same copy ran at 20-40 GB/s
+    // (by every sign bound by the GPU's translations of the caller's pages),
+    // below the staging ring's ~80 GB/s, which a host-side memcpy feeds.
+    // After such a copy the next 8 large ones take the ring, then the kernel
+    // is tried again.
+    if (h->hr_bytes) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, h->hr_ev[0], h->hr_ev[1]) == cudaSuccess && ms > 0.f &&
+          (double)h->hr_bytes / (ms * 1e6) < 70.0)
+        h->hr_skip = 8;
+      cudaGetLastError();
+      h->hr_bytes = 0;
+    }
+    if (h->hr_skip) {
+      --h->hr_skip;
+      kernel = false;
+    } else {
+      for (auto& e : h->hr_ev)
+        if (!e && cudaEventCreate(&e) != cudaSuccess) e = nullptr;
+      cudaGetLastError();
+      timed = h->hr_ev[0] && h->hr_ev[1];
+    }
+  }
+  if (kernel) {
     const size_t n16 = bytes / 16;
     const unsigned grid = (unsigned)std::min<size_t>((size_t)h->sms * 8, (n16 + 255) / 256);
+    if (timed) MCK(cudaEventRecord(h->hr_ev[0], h->stream));
     k_copy_from_host<<<grid, 256, 0, h->stream>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), n16);
     launched(h, "copy_from_host");
+    if (timed) {
+      MCK(cudaEventRecord(h->hr_ev[1], h->stream));
+      h->hr_bytes = bytes;
+    }
     if (bytes % 16)
       MCK(cudaMemcpyAsync(static_cast<unsigned char*>(dst) + n16 * 16, static_cast<const unsigned char*>(src) + n16 * 16,
                           bytes % 16, cudaMemcpyHostToDevice, h->stream));
@@ -2164,6 +2196,8 @@ mistic_status mistic_destroy(mistic_handle h) {
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : h->jev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : h->hr_ev)
     if (e) cudaEventDestroy(e);
   if (h->own_stream) cudaStreamDestroy(h->stream);
   for (mistic_handle w : h->workers) mistic_destroy(w);
