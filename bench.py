@@ -339,6 +339,8 @@ def run_mistic(args, wl) -> None:
     # GPU FP64 brute force (mistic_bruteforce_rows) against the degrees of
     # the timed run's pair list
     verify = None
+    if args.verify_rows < 0:  # default: 16,384 rows where the brute force takes seconds (n * d <= 2e8)
+        args.verify_rows = 16384 if n * d <= 2e8 else 0
     if args.verify_rows > 0:
         pr = pbuf[:r.pairs_ij]
         deg = torch.zeros(n, dtype=torch.int64, device=dev)
@@ -820,8 +822,9 @@ def main() -> None:
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--fp64-rows", type=int, default=0,
                     help="time the plain FP64 comparison on the first N rows only (0: all rows)")
-    ap.add_argument("--verify-rows", type=int, default=0,
-                    help="check the neighbour counts of this many rows against the GPU FP64 brute force")
+    ap.add_argument("--verify-rows", type=int, default=-1,
+                    help="check the neighbour counts of this many rows against the GPU FP64 brute force "
+                         "(default: 16,384 where n * d <= 2e8, else none)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-c5", action="store_true", help="skip the 5M x 384 north-star measurement")
