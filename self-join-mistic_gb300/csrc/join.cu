@@ -364,8 +364,12 @@ k_join_f32(const JoinParams P) {
 // FP32 filter for d <= 32: the lane's candidate row lives in registers as DQ
 // float4 chunks (compile time), the home rows are visited in groups of 8 so
 // each shared-memory broadcast load feeds 8 independent FMA chains, and each
-// group is classified as soon as it is complete (8 live accumulators).
-template <int DQ>
+// group is classified as soon as it is complete (8 live accumulators).  HALF:
+// the last chunk's second coordinate pair is padding (d <= 4 DQ - 2) and is
+// skipped -- its terms are (0 - 0)^2, so the sums are unchanged (5M x 18:
+// 30.6 -> 28.6 ms; groups of 2 and 6 rows for the last rows of small bins
+// were measured slower, 31.9 ms).
+template <int DQ, bool HALF>
 __global__ void __launch_bounds__(JOIN_THREADS, (DQ <= 4 ? 4 : 3))
 k_join_f32r(const JoinParams P) {
   constexpr int CH = 32;
@@ -415,12 +419,18 @@ k_join_f32r(const JoinParams P) {
         for (int c = 0; c < DQ; ++c) {
 #pragma unroll
           for (int i = 0; i < NR; ++i) {
-            const ulonglong2 aa = reinterpret_cast<const ulonglong2*>(sA)[(r0 + i) * DQ + c];
             unsigned long long tt;
-            asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(tt) : "l"(aa.x), "l"(qq[c].x));
-            asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[i]) : "l"(tt));
-            asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(tt) : "l"(aa.y), "l"(qq[c].y));
-            asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[i]) : "l"(tt));
+            if (HALF && c == DQ - 1) {
+              const unsigned long long ax = reinterpret_cast<const unsigned long long*>(sA)[2 * ((r0 + i) * DQ + c)];
+              asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(tt) : "l"(ax), "l"(qq[c].x));
+              asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[i]) : "l"(tt));
+            } else {
+              const ulonglong2 aa = reinterpret_cast<const ulonglong2*>(sA)[(r0 + i) * DQ + c];
+              asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(tt) : "l"(aa.x), "l"(qq[c].x));
+              asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[i]) : "l"(tt));
+              asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(tt) : "l"(aa.y), "l"(qq[c].y));
+              asm("fma.rn.f32x2 %0, %1, %1, %0;" : "+l"(acc2[i]) : "l"(tt));
+            }
           }
         }
 #pragma unroll
@@ -434,8 +444,9 @@ k_join_f32r(const JoinParams P) {
       };
 #pragma unroll
       for (int g = 0; g < CH / 8; ++g) {
-        if (g * 8 >= (int)na) break;
-        if ((int)na - g * 8 <= 4)
+        const int left = (int)na - g * 8;  // warp-uniform
+        if (left <= 0) break;
+        if (left <= 4)
           rows(std::integral_constant<int, 4>{}, g * 8);
         else
           rows(std::integral_constant<int, 8>{}, g * 8);
@@ -680,16 +691,27 @@ void run(mistic_handle_s* h, bool fp64, int CH, const JoinParams& P) {
   if (!fp64) {
     const size_t spw = (size_t)CH * P.dpad * sizeof(float);
     if (CH == 32 && P.dpad <= 32) {
+      // the last float4 chunk holds at most two coordinates: skip its padding pair
+      const bool half = P.d + 2 <= P.dpad;
+#define MISTIC_F32R(DQ)                                                              \
+  case DQ:                                                                           \
+    if (half)                                                                        \
+      launch_persistent(h, k_join_f32r<DQ, true>, spw, P, "join_f32r");              \
+    else                                                                             \
+      launch_persistent(h, k_join_f32r<DQ, false>, spw, P, "join_f32r");             \
+    return;
       switch (P.dpad / 4) {
-        case 1: launch_persistent(h, k_join_f32r<1>, spw, P, "join_f32r"); return;
-        case 2: launch_persistent(h, k_join_f32r<2>, spw, P, "join_f32r"); return;
-        case 3: launch_persistent(h, k_join_f32r<3>, spw, P, "join_f32r"); return;
-        case 4: launch_persistent(h, k_join_f32r<4>, spw, P, "join_f32r"); return;
-        case 5: launch_persistent(h, k_join_f32r<5>, spw, P, "join_f32r"); return;
-        case 6: launch_persistent(h, k_join_f32r<6>, spw, P, "join_f32r"); return;
-        case 7: launch_persistent(h, k_join_f32r<7>, spw, P, "join_f32r"); return;
-        default: launch_persistent(h, k_join_f32r<8>, spw, P, "join_f32r"); return;
+        MISTIC_F32R(1)
+        MISTIC_F32R(2)
+        MISTIC_F32R(3)
+        MISTIC_F32R(4)
+        MISTIC_F32R(5)
+        MISTIC_F32R(6)
+        MISTIC_F32R(7)
+        MISTIC_F32R(8)
+        default: break;
       }
+#undef MISTIC_F32R
     }
     if (CH == 32)
       launch_persistent(h, k_join_f32<32>, spw, P, "join_f32");
