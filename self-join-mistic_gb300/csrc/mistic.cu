@@ -211,11 +211,19 @@ PinnedCache& pinned_cache() {
   return *c;
 }
 
-// A pinned block owned by a call until it is handed to the result.
+// A pinned block owned by a call until it is handed to the result.  Kernels
+// of the call's stream may write it (host pair lists): before it goes back
+// to the cache -- a larger one replacing it, or an error unwinding the call --
+// the stream is drained.
 struct PinnedHold {
   void* p = nullptr;
+  cudaStream_t stream = nullptr;
   void reset() {
-    if (p) pinned_cache().release(p);
+    if (p) {
+      cudaStreamSynchronize(stream);
+      cudaGetLastError();
+      pinned_cache().release(p);
+    }
     p = nullptr;
   }
   ~PinnedHold() { reset(); }
@@ -1442,6 +1450,7 @@ void run_selfjoin(mistic_handle h, const void* pts, uint64_t n, uint32_t d, mist
   // in the result's (i, j) order, and no copy follows the join.
   bool host_direct = want_pairs && o.pairs == MISTIC_PAIRS_HOST && !o.sort_pairs && !want_csr && h->host_pairs;
   PinnedHold hold;
+  hold.stream = h->stream;
   auto host_list = [&](unsigned long long c) -> unsigned long long* {
     hold.reset();
     hold.p = pinned_cache().acquire(std::max<size_t>(8, c * 8));
@@ -2300,6 +2309,10 @@ mistic_status mistic_batch_selfjoin(mistic_handle h, const mistic_instance* inst
       msg = e.what();
     }
     if (st != MISTIC_OK) {
+      // copies into the results' blocks may still be in flight: let them
+      // land before the blocks go back to the pinned cache
+      cudaStreamSynchronize(h->stream);
+      cudaGetLastError();
       for (uint32_t i = 0; i < m; ++i) mistic_result_free(&results[i]);
       return fail(h, st, msg.empty() ? mistic_strerror(st) : msg.c_str());
     }
