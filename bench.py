@@ -23,7 +23,7 @@ of the dominant kernel, the whole step against its lower bound, and a CPU
 baseline (the reference's brute-force algorithm, src/utils.cu:285-317, as
 the oracle's C port, on a bounded row sample, extrapolated to the whole job).
 
-The line also carries the benchmark spec: the 5M x 384 clustered FP32 workload
+The line also carries `tiny384_5m`: the 5M x 384 clustered FP32 workload
 (TINY-shaped, k = 8, 16 mean neighbours) measured in the same run -- mixed
 precision at full size, and mixed precision against the plain FP64 join
 (and TF32) on a fixed full-density sample of home points (mistic_opts.
@@ -443,7 +443,7 @@ def run_mistic(args, wl) -> None:
                 "peak_source": "mistic_peaks FFMA probe, this run (CUDA-core FP32 pipe)"}
     roof["hbm_peak_gbs"] = peaks.get("hbm_gbs")
     step_roof = step_lower_bound(r, n, d, wl.k, ms, peaks)
-    north = None if (args.no_c5 or args.workload == "tiny384") else run_north_star(h, args, dev, stream, peaks)
+    big384 = None if (args.no_tiny384 or args.workload == "tiny384") else run_tiny384_full(h, args, dev, stream, peaks)
     cpu = cpu_sample(x, wl.eps, args.cpu_seconds) if not args.no_cpu else None
     host = host_join_sample(x, wl.eps, wl.k, args.cpu_seconds) if not args.no_cpu else None
     ref_gpu = reference_gpu(x, wl.k, wl.eps, r.pairs_ordered_incl_self, args.ref_gpu_timeout) \
@@ -468,7 +468,7 @@ def run_mistic(args, wl) -> None:
         "verify": verify,
         "roofline": roof,
         "step_roofline": step_roof,
-        "north_star": north,
+        "tiny384_5m": big384,
         "reference_gpu": ref_gpu,
         "e2e": {"value": job_points_per_s(n, world, e2e_ms), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": n * d * x.itemsize, "d2h_bytes_per_step": int(r.pairs_ij) * 8,
@@ -547,16 +547,16 @@ def step_lower_bound(r, n: int, d: int, k: int, ms: float, peaks: dict) -> dict:
             "model": "index bytes/HBM + max(2*ceil16(d) flops per candidate / BF16, 8 B per pair / HBM)"}
 
 
-def run_north_star(h, args, dev, stream, peaks) -> dict:
+def run_tiny384_full(h, args, dev, stream, peaks) -> dict:
     """The 5M x 384 clustered FP32 workload in the same run: mixed precision
-    at full size (args.c5_steps timed steps after one warm-up), then mixed
+    at full size (args.tiny384_steps timed steps after one warm-up), then mixed
     precision, plain FP64 and TF32 on one full-density sample of home points
     (mistic_opts.home_sample, about 1.5e10 candidate pairs), pair sets
     compared on the device."""
     import torch
     from mistic import _lib as L
     t0 = time.perf_counter()
-    wl = W.tiny384(args.c5_n or 5_000_000)
+    wl = W.tiny384(args.tiny384_n or 5_000_000)
     gen_s = time.perf_counter() - t0
     x = np.ascontiguousarray(wl.pts)
     n, d = x.shape
@@ -575,10 +575,10 @@ def run_north_star(h, args, dev, stream, peaks) -> dict:
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    res = [call(o_dev) for _ in range(args.c5_steps)]
+    res = [call(o_dev) for _ in range(args.tiny384_steps)]
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.c5_steps
+    ms = e0.elapsed_time(e1) / args.tiny384_steps
     r = res[-1]
     tc_ms = statistics.mean(q.ms["join_tc"] for q in res)
     kd = {"split-bf16": (d + 31) // 32 * 32, "bf16": (d + 63) // 64 * 64, "tf32": (d + 31) // 32 * 32}.get(
@@ -593,7 +593,7 @@ def run_north_star(h, args, dev, stream, peaks) -> dict:
             "kernel_ms": tc_ms, "cells": r.tc_cells,
             "work": "2*d flops per evaluated cell; issued = tiles x 128 x 128 x products x 2 x K"}
     # ---- the same full-density sample in every mode
-    S = max(1, int(round(r.candidates / args.c5_sample_cands)))
+    S = max(1, int(round(r.candidates / args.tiny384_sample_cands)))
     cap_s = max(1 << 20, int(r.pairs_ij / max(1, S) * 4) + 4096)
     bufs = {}
     out = {}
@@ -616,7 +616,7 @@ def run_north_star(h, args, dev, stream, peaks) -> dict:
     line = {
         "workload": "tiny384", "n": n, "d": d, "k": wl.k, "eps_hex": float(wl.eps).hex(),
         "desc": WORKLOADS["tiny384"][1], "generation_s": gen_s,
-        "steps": args.c5_steps, "warmup": 1, "ms_per_step": ms, "value": n / (ms * 1e-3), "unit": UNIT,
+        "steps": args.tiny384_steps, "warmup": 1, "ms_per_step": ms, "value": n / (ms * 1e-3), "unit": UNIT,
         "mode_used": r.mode_used, "tc_operands": r.tc_operands, "tc_kernel": r.tc_kernel,
         "tc_min_bin": r.tc_min_bin, "tuned": r.tuned,
         "pairs_ij": r.pairs_ij, "candidates": r.candidates, "band_pairs": r.band_pairs,
@@ -646,7 +646,7 @@ def run_north_star(h, args, dev, stream, peaks) -> dict:
 
 
 def run_batch(args) -> None:
-    """c4: 2,000 independent instances (n log-uniform in [1e3, 2e5], d in
+    """The batch: 2,000 independent instances (n log-uniform in [1e3, 2e5], d in
     {2,8,18,32,57,90}, FP32 Gaussian mixtures) through one
     mistic_batch_selfjoin call per step.  value: inputs resident in HBM,
     counts only; e2e: host inputs and host pair lists.  The batch call is
@@ -827,11 +827,11 @@ def main() -> None:
                          "(default: 16,384 where n * d <= 2e8, else none)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--no-c5", action="store_true", help="skip the 5M x 384 north-star measurement")
-    ap.add_argument("--c5-n", type=int, default=0, help="points of the north-star workload (default 5,000,000)")
-    ap.add_argument("--c5-steps", type=int, default=2, help="timed full-size steps of the north-star workload")
-    ap.add_argument("--c5-sample-cands", type=float, default=1.5e10,
-                    help="candidate pairs of the north-star mixed/FP64 sample")
+    ap.add_argument("--no-tiny384", action="store_true", help="skip the nested 5M x 384 measurement")
+    ap.add_argument("--tiny384-n", type=int, default=0, help="points of the nested 5M x 384 workload (default 5,000,000)")
+    ap.add_argument("--tiny384-steps", type=int, default=2, help="timed full-size steps of the nested 5M x 384 workload")
+    ap.add_argument("--tiny384-sample-cands", type=float, default=1.5e10,
+                    help="candidate pairs of the nested 5M x 384 workload's mixed/FP64 sample")
     ap.add_argument("--ref-seconds", type=float, default=6.0)
     ap.add_argument("--ref-gpu", action="store_true",
                     help="also run the reference's own GPU build (oracle/build_ref_gpu.sh) on the same points")
@@ -840,7 +840,7 @@ def main() -> None:
     if args.workload == "batch2000":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the single-instance "
-                              "workloads; c4 reports its CPU baseline in the mistic line"}), flush=True)
+                              "workloads; the batch reports its CPU baseline in the mistic line"}), flush=True)
         else:
             run_batch(args)
         return

@@ -91,7 +91,7 @@ CASES = [
 ]
 
 
-# Full-size cases (the c1 workload: n = 100,000, d = 18, U[0,1) from seed 0,
+# Full-size cases (the uniform workload: n = 100,000, d = 18, U[0,1) from seed 0,
 # ε calibrated to 32 mean neighbours).  `--full` (re)computes only these and
 # keeps the small cases; the reference's brute force takes about 30 s here.
 FULL_CASES = [

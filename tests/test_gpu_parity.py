@@ -39,8 +39,8 @@ def test_golden_case(handle, golden, idx, mode):
 
 
 @pytest.mark.parametrize("mode", MODES)
-def test_c1_full_size(handle, golden_full, mode):
-    """The c1 workload at full size (n = 100,000, d = 18): the reference's
+def test_uniform_100k_full_size(handle, golden_full, mode):
+    """The uniform workload at full size (n = 100,000, d = 18): the reference's
     own brute-force count and the oracle's pair-list hash, in every mode."""
     c = golden_full[0]
     x = case_input(c)

@@ -36,7 +36,7 @@ def test_oracle_matches_reference_counts(golden, idx):
 
 
 def test_full_size_pin_is_consistent(golden_full):
-    """The c1 pin (reference brute force over 100,000 x 18 points): its input
+    """The full-size pin (reference brute force over 100,000 x 18 points): its input
     regenerates bit-for-bit here, and the reference's ordered count equals
     2 x the oracle's i<j pairs + n."""
     c = golden_full[0]
