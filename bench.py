@@ -443,9 +443,18 @@ def run_mistic(args, wl) -> None:
                 "peak_source": "mistic_peaks FFMA probe, this run (CUDA-core FP32 pipe)"}
     roof["hbm_peak_gbs"] = peaks.get("hbm_gbs")
     step_roof = step_lower_bound(r, n, d, wl.k, ms, peaks)
-    big384 = None if (args.no_tiny384 or args.workload == "tiny384") else run_tiny384_full(h, args, dev, stream, peaks)
-    cpu = cpu_sample(x, wl.eps, args.cpu_seconds) if not args.no_cpu else None
-    host = host_join_sample(x, wl.eps, wl.k, args.cpu_seconds) if not args.no_cpu else None
+    # the nested and baseline measurements report a failure in their own
+    # field rather than take the headline line down with them
+    def guarded(fn, *a):
+        try:
+            return fn(*a)
+        except Exception as e:  # noqa: BLE001
+            return {"error": f"{type(e).__name__}: {e}"[:300]}
+
+    big384 = None if (args.no_tiny384 or args.workload == "tiny384") else \
+        guarded(run_tiny384_full, h, args, dev, stream, peaks)
+    cpu = guarded(cpu_sample, x, wl.eps, args.cpu_seconds) if not args.no_cpu else None
+    host = guarded(host_join_sample, x, wl.eps, wl.k, args.cpu_seconds) if not args.no_cpu else None
     ref_gpu = reference_gpu(x, wl.k, wl.eps, r.pairs_ordered_incl_self, args.ref_gpu_timeout) \
         if args.ref_gpu else None
     value = job_points_per_s(n, world, ms)
@@ -475,7 +484,7 @@ def run_mistic(args, wl) -> None:
                 "h2d_ms": statistics.mean(t[1] for t in e2e_res), "d2h_ms": statistics.mean(t[2] for t in e2e_res)},
         "gpu_launches": launches,
         "clocks": clk,
-        "cpu_baseline": None if cpu is None else {
+        "cpu_baseline": cpu if (cpu is None or "error" in cpu) else {
             "value": cpu["points_per_s"], "unit": UNIT, "cores": cpu["threads"], "kind": "port",
             "sample": f"rows [0,{cpu['rows']}) x all {n} rows ({cpu['seconds']:.1f} s), extrapolated to "
                       f"n rows; brute_force of src/utils.cu:285-317 (oracle C port, OpenMP)",
